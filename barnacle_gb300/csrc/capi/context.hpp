@@ -1,0 +1,76 @@
+// bn_context: the device-resident state behind the C-ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../../include/barnacle_gpu.h"
+#include "../device/dev_types.cuh"
+#include "../device/launch.hpp"
+
+// growable device buffer
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t reserve(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(ptr); }
+};
+
+struct bn_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+  std::string err;
+
+  // scene
+  bool has_scene = false;
+  bn::DevScene scene{};
+  DevBuf nodes, tris, inst, mats, lights, light_inst, tri_pdf, tri_lights, error_word, counters;
+  std::vector<int32_t> inst_order;     // TLAS order -> descriptor index
+  std::vector<bn::DevMaterial> host_mats;
+  std::vector<int32_t> host_inst_light;  // per TLAS instance: light index
+  int n_lights = 0;
+
+  // queries
+  DevBuf q_in, q_out;
+
+  // render
+  DevBuf views, item_offsets, partial, film, wf_state;
+  long long film_floats = 0;
+  bn_stats stats{};
+
+  // pssmlt / adjoint scratch
+  DevBuf mlt_state, mlt_boot, mlt_chain, adj_params, adj_image, adj_target, adj_grad, adj_aux;
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? BN_ERR_OUT_OF_MEMORY : BN_ERR_CUDA;
+  }
+};
+
+namespace bnc {
+// host-side view constants (Extensions/Camera/Pinhole.fs:16-22), shared by all render modes
+bn::DevView make_dev_view(const bn_view& v, long long pixel_offset, long long path_offset);
+int check_device_error(bn_context* ctx);
+int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views);
+int render_pssmlt(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views);
+}  // namespace bnc

@@ -1,0 +1,97 @@
+// Device-resident scene layout (HBM), written once by bn_scene_upload.
+//
+//  nodes      2 x float4 per BVHNode, the reference's 32-byte layout (Util/BVH.fs:52-73):
+//             n0 = (min.x, min.y, min.z, max.x), n1 = (max.y, max.z, int right|offset,
+//             int bytes [is_leaf, split_axis, count, mask]).  TLAS first (root 0), then every
+//             mesh's BLAS at DevInstance::node_base.  Loaded as two 16-byte vector loads.
+//  tris       3 x float4 per triangle in BLAS-permuted order, all meshes back to back:
+//             (p0, material slot or -1), (p1, original index), (p2, 0).  48 bytes = the 12-byte
+//             index + 36 bytes of vertices the reference gathers per tested triangle.
+//  instances  DevInstance in TLAS-permuted order (BVHAggregate permutes its array in place).
+//  materials  DevMaterial (32 B), lights DevLight (16 B).
+//  light tables:
+//    uniform (Extensions/LightSampler/Uniform.fs): light_inst[] = emissive instances in TLAS
+//      order; tri_pdf[global tri] = the reference AliasTable entry pdf of each mesh triangle
+//      (area / sum of areas in object space, Util/AliasTable.fs:14-27 + Mesh.fs:181-186).
+//    alias-triangles (new plugin): Vose table over all emissive (instance, triangle) pairs,
+//      entries DevTriLight; DevInstance::light_entry_base maps a hit back to its entry.
+#pragma once
+#include <cstdint>
+
+namespace bn {
+
+enum : int { kPrimMesh = 0, kPrimSphere = 1 };
+enum : int { kMatLambertian = 0, kMatMirror = 1, kMatDielectric = 2, kMatPBR = 3 };
+
+struct alignas(16) DevInstance {
+  float4 bmin;      // world AABB min, .w unused
+  float4 bmax;      // world AABB max, .w = sphere radius
+  float4 w2o[3];    // w2o[r] = (M1r, M2r, M3r, M4r) of WorldToObject: x'_r = ((x*M1r + y*M2r) + z*M3r) + M4r
+  float4 o2w[3];    // same for ObjectToWorld
+  int prim_type;    // kPrimMesh / kPrimSphere
+  int node_base;    // BLAS root in nodes[]
+  int tri_base;     // first triangle of the mesh in tris[]
+  int n_tris;
+  int material;     // -1 = no material (a light only; the path ends there)
+  int light;        // -1 = not emissive
+  int light_entry_base;  // alias-triangles: entry index of triangle 0 of this instance, -1 if none
+  int mesh;         // mesh id (debug/statistics)
+};
+static_assert(sizeof(DevInstance) == 160, "DevInstance layout");
+
+struct alignas(16) DevMaterial {
+  int type;
+  float base[3];
+  float ior;
+  float alpha;     // max(roughness^2, 1e-3) (PBR.fs:106)
+  float metallic;  // clamp(metallic, 0, 1) (PBR.fs:107)
+  float roughness;
+};
+static_assert(sizeof(DevMaterial) == 32, "DevMaterial layout");
+
+struct alignas(16) DevLight {
+  float emission[3];
+  int two_sided;
+};
+
+struct alignas(16) DevTriLight {
+  float prob;       // Vose acceptance probability
+  int alias;        // Vose alias entry
+  float pmf;        // probability of picking this entry
+  float area;       // world-space area
+  int inst;         // instance (TLAS order)
+  int tri;          // triangle within the mesh (BLAS order)
+  int pad0, pad1;
+};
+
+struct DevView {
+  float ul[3], du[3], dv[3];  // pinhole viewport: upper-left, pixel deltas (Pinhole.fs:12-27)
+  float c2w[16];              // CameraToWorld
+  int width, height;
+  int cam_type;
+  float aperture, focus_distance, push_forward;
+  long long pixel_offset;     // first pixel of this view in the concatenated film
+  long long path_offset;      // first path id of this view (pixels * spp before it)
+};
+
+struct DevScene {
+  const float4* __restrict__ nodes;
+  const float4* __restrict__ tris;
+  const DevInstance* __restrict__ inst;
+  const DevMaterial* __restrict__ mats;
+  const DevLight* __restrict__ lights;
+  const int* __restrict__ light_inst;     // uniform sampler: emissive instances
+  const float* __restrict__ tri_pdf;      // uniform sampler: reference alias pdf per triangle
+  const DevTriLight* __restrict__ tri_lights;  // alias-triangles sampler
+  int n_inst;
+  int n_tlas_nodes;
+  int n_nodes;
+  int n_tris;
+  int n_light_inst;
+  int n_tri_lights;
+  int light_sampler;                      // 0 uniform, 1 alias-triangles
+  int n_mats;
+  unsigned int* error_word;               // BN_DEVERR_* bits
+};
+
+}  // namespace bn

@@ -1,0 +1,40 @@
+// Host-side launchers of the device kernels (one translation unit per kernel family).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../../include/barnacle_gpu.h"
+#include "dev_types.cuh"
+
+namespace bn {
+
+// per-launch counters written by kernels that count (BN_TRACE_COUNT, stats renders)
+struct DevCounters {
+  unsigned long long rays, nodes, tris, insts, paths, accepted, proposed, pad;
+};
+
+cudaError_t launch_trace(const DevScene& s, const bn_ray* rays, bn_hit* hits, long long n, unsigned flags,
+                         DevCounters* counters, cudaStream_t st);
+cudaError_t launch_bsdf(const DevScene& s, const bn_bsdf_query* q, bn_bsdf_result* out, long long n, bool sample,
+                        cudaStream_t st);
+cudaError_t launch_sampler_stream(const uint32_t* seeds, long long n_streams, int n_draws, float* out, cudaStream_t st);
+
+// Plain megakernel: one thread per (view, pixel, sample chunk); partial sums per chunk, then a
+// reduction in chunk order into the FP32 film (rows flipped as Film.SetPixel does).
+struct MegaParams {
+  const DevView* views;
+  int n_views;
+  long long n_items;         // sum over views of pixels * chunks
+  const long long* item_offsets;  // per view: first item (device)
+  int spp, chunks, spc;      // samples per pixel, chunks per pixel, samples per chunk
+  int max_depth, rr_depth, frame_id;
+  bool watertight;
+  bool count;
+  float4* partial;           // n_items partial sums (scratch)
+  float* film;               // concatenated views, 3 floats per pixel
+  long long n_pixels;
+  DevCounters* counters;
+};
+cudaError_t launch_megakernel(const DevScene& s, const MegaParams& p, cudaStream_t st);
+cudaError_t launch_mega_reduce(const MegaParams& p, cudaStream_t st);
+
+}  // namespace bn

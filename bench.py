@@ -1,0 +1,314 @@
+"""Benchmark of the render call on the 1,024-instance, 16-view workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--mode wavefront|megakernel]
+                  [--impl reference] [--spp-per-step S]
+
+A step renders every one of the 16 views (256x240 ... 1920x1080, ~13 M pixels) at S samples per
+pixel (the workload's 64 spp = 64 / S steps), max depth 12, Russian roulette from depth 3, the
+alias-table light sampler over the 64 emissive triangles.  The scene (630 k unique / 163 M
+instanced triangles, 1,089 instances) is resident in HBM; L2 is flushed (a 512 MiB write)
+before every timed step.
+
+value  = paths / device time (CUDA events on the library's stream around its kernels).
+e2e    = the same metric through bn_render with a host output buffer: the views' descriptors
+         go host->device and the FP32 film comes back device->host inside the timed region.
+roofline: the dominant kernel's algorithmic bytes (32 per BVH node tested, 48 per triangle
+         tested, 152 per instance visited, counted by an instrumented run of the same step) over
+         its event-timed duration, against the measured HBM copy bandwidth.
+--impl reference: the CPU restatement of the reference path (the F# renderer cannot be built
+         here) on all host cores, each step a bounded sample of the same workload.
+Multi-GPU (torchrun): every rank renders the full workload (replicas, weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "paths/sec at equal image RMSE: batched wavefront vs plain megakernel; adjoint/fwd"
+WORKLOAD = "instances"
+
+
+def bytes_per_unit():
+    return {"node": 32, "triangle": 48, "instance": 152}
+
+
+def measured_peak_gbs():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_render(bundle, render, spp, views, crop_size, threads):
+    """Times the oracle (CPU restatement) on crops of the given views; returns (paths, seconds)."""
+    from oracle import pyoracle
+
+    osc = pyoracle.Scene(bundle.scene)
+    r = render
+    r.spp = spp
+    paths, secs = 0, 0.0
+    for v in views:
+        cw, ch = min(crop_size, v.width), min(crop_size, v.height)
+        x0, y0 = (v.width - cw) // 2, (v.height - ch) // 2
+        t0 = time.perf_counter()
+        osc.render_pt(r, v, crop=(x0, y0, x0 + cw, y0 + ch), threads=threads)
+        secs += time.perf_counter() - t0
+        paths += cw * ch * spp
+    return paths, secs
+
+
+def run_reference(args, world, rank, dist):
+    """--impl reference: the CPU restatement on all host threads, bounded samples per step."""
+    if rank != 0:
+        return
+    from barnacle_gb300 import Bundle
+
+    b = Bundle.generate(WORKLOAD, 1)
+    views = b.views
+    threads = os.cpu_count() or 1
+    r = b.render
+    sample_views = views[:4]
+    crop = 48
+    for _ in range(args.warmup):
+        cpu_sample_render(b, b.render, args.spp_per_step, sample_views[:1], 16, threads)
+    paths, secs = 0, 0.0
+    for _ in range(args.steps):
+        p, s = cpu_sample_render(b, b.render, args.spp_per_step, sample_views, crop, threads)
+        paths += p
+        secs += s
+    value = paths / secs
+    line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "impl": "reference",
+            "config": {"workload": f"{WORKLOAD}: 1024 instances of 4 displaced icospheres + 64 emissive triangles, "
+                                   "16 views, depth 12, rr 3", "spp_per_step": args.spp_per_step,
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+                             "sample": f"{crop}x{crop} centre crops of 4 of the 16 views x {args.spp_per_step} spp "
+                                       f"per step (the F# reference cannot be built: no .NET SDK)"},
+            "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        return
+    import torch
+
+    from barnacle_gb300 import Bundle, Context, capi
+
+    dev = local if world > 1 else 0
+    ctx = Context(dev)
+    b = Bundle.generate(WORKLOAD, 1)
+    ctx.upload(b)
+    views = b.views
+    r = b.render
+    r.spp = args.spp_per_step
+    r.mode = capi.BN_MODE_WAVEFRONT if args.mode == "wavefront" else capi.BN_MODE_MEGAKERNEL
+    pixels = sum(v.width * v.height for v in views)
+    paths_per_step = pixels * r.spp
+    torch.cuda.set_device(dev)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    # algorithmic bytes per launch of the dominant kernel: an instrumented run of one step
+    rc = capi.bn_render_desc()
+    C_copy = bytes(r)
+    import ctypes as C
+    C.memmove(C.addressof(rc), C_copy, len(C_copy))
+    rc.flags |= capi.BN_RENDER_COUNT
+    rc.frame_id = 10_000
+    ctx.reset_stats()
+    ctx.render(rc, views, to_host=False)
+    st = ctx.stats()
+    bpu = bytes_per_unit()
+    alg_bytes = bpu["node"] * st.nodes_visited + bpu["triangle"] * st.tris_tested + bpu["instance"] * st.instances_visited
+    rays_per_step = st.rays
+
+    for w in range(args.warmup):
+        r.frame_id = w
+        ctx.render(r, views, to_host=False)
+    barrier(dist)
+    torch.cuda.synchronize()
+    dev_ms, dom_ms, launches = 0.0, 0.0, 0
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r.frame_id = 100 + k
+            ctx.render(r, views, to_host=False)
+            s = ctx.stats()
+            dev_ms += s.last_kernel_ms
+            dom_ms += s.last_dominant_ms
+            launches += s.last_launches
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    dev_s = max_over_ranks(dist, dev_ms / 1000.0)
+
+    # end to end through the C-ABI with a host film (pinned)
+    film = torch.empty(pixels * 3, dtype=torch.float32).pin_memory().numpy()
+    view_arr = (capi.bn_view * len(views))(*views)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        r.frame_id = 200 + k
+        rcode = ctx.lib.bn_render(ctx._h, C.byref(r), view_arr, len(views), capi.ptr(film))
+        if rcode:
+            raise RuntimeError(ctx.error())
+        float(film[0])  # the step's result is on the host
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+
+    peak, peak_kind = measured_peak_gbs()
+    dom_launch_s = dom_ms / 1000.0 / args.steps
+    achieved = alg_bytes / dom_launch_s / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / f"traffic_{args.mode}_{WORKLOAD}.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("bytes_per_launch")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        p, s = cpu_sample_render(b, b.render, args.spp_per_step, views[:4], 48, threads)
+        cpu = {"value": p / s, "unit": "paths/s", "cores": threads, "kind": "port",
+               "sample": f"48x48 centre crops of 4 of the 16 views x {args.spp_per_step} spp "
+                         "(oracle: CPU restatement of the F# path; the F# renderer cannot be built here)"}
+
+    if rank == 0:
+        value = world * paths_per_step * args.steps / dev_s
+        line = {
+            "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": f"{WORKLOAD}: 1024 instances of 4 displaced icospheres (20k/82k/200k/328k tris) "
+                                   "+ 64 emissive triangles, 16 views 256x240..1920x1080, depth 12, rr 3",
+                       "mode": args.mode, "spp_per_step": r.spp, "pixels_per_step": pixels,
+                       "rays_per_step": int(rays_per_step), "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed before every timed step (512 MiB write)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_pt_mega" if args.mode == "megakernel" else "wavefront extend",
+                         "alg_bytes_per_launch": int(alg_bytes)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * paths_per_step * args.steps / e2e_s, "unit": "paths/s",
+                    "h2d_bytes_per_step": C.sizeof(capi.bn_view) * len(views),
+                    "d2h_bytes_per_step": pixels * 3 * 4},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "mrays_per_s": world * rays_per_step * args.steps / dev_s / 1e6,
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

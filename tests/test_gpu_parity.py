@@ -1,0 +1,298 @@
+"""GPU parity: the CUDA path (through the C-ABI) against the CPU oracle on the same inputs.
+
+Bars (from the porting contract of the render call):
+  * ray queries: closest-hit instance and triangle ids bit-exact, t and (u, v) bit-exact (the
+    device path uses the oracle's operation order), any-hit answers identical;
+  * BSDF value and pdf within 1e-5 relative of the FP64 oracle;
+  * images: per-pixel means within 3 standard errors of the oracle's estimate, RMSE at equal spp
+    within a few percent; specular-only scenes (no transcendental functions on the path) render
+    bit-identically.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from barnacle_gb300 import BarnacleError, Bundle, capi
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+SCENES = ["cornell", "cornell-objects", "materials", "instances"]
+
+
+def random_rays(n, lo, hi, rng, t_max=np.inf):
+    r = np.zeros(n, capi.RAY_DTYPE)
+    r["origin"] = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.sqrt((d.astype(np.float32) ** 2).sum(1, dtype=np.float32))[:, None]
+    r["direction"] = d
+    r["t_max"] = t_max
+    return r
+
+
+def scene_rays(bundle, n, rng):
+    """Camera-origin rays toward random scene points, random interior rays and axis-aligned
+    rays (exact zero direction components exercise the infinite reciprocals of the slab test)."""
+    v = bundle.views[0]
+    eye = np.array(list(v.camera.camera_to_world)[12:15], np.float32)
+    if bundle.scene.contents.n_instances > 100:
+        lo, hi = np.array([-60, 0, -60], np.float32), np.array([60, 25, 60], np.float32)
+    else:
+        lo, hi = np.zeros(3, np.float32), np.ones(3, np.float32)
+    a = random_rays(n, lo, hi, rng)
+    b = np.zeros(n, capi.RAY_DTYPE)
+    b["origin"] = eye
+    tgt = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    d = (tgt - eye).astype(np.float32)
+    b["direction"] = d / np.sqrt((d ** 2).sum(1, dtype=np.float32))[:, None]
+    b["t_max"] = np.inf
+    c = random_rays(n // 4, lo, hi, rng)
+    axes = np.eye(3, dtype=np.float32)[rng.integers(0, 3, n // 4)] * rng.choice([-1, 1], size=(n // 4, 1))
+    c["direction"] = axes.astype(np.float32)
+    return np.concatenate([a, b, c])
+
+
+@pytest.fixture(scope="module")
+def loaded():
+    cache = {}
+
+    def get(ctx, name):
+        if name not in cache:
+            b = Bundle.generate(name, 1)
+            cache[name] = (b, pyoracle.Scene(b.scene))
+        b, o = cache[name]
+        ctx.upload(b)
+        return b, o
+
+    return get
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_tlas_order_matches_oracle(ctx, loaded, name):
+    b, o = loaded(ctx, name)
+    n = b.scene.contents.n_instances
+    _, order = o.tlas()
+    assert np.array_equal(ctx.instance_order(n), order)
+
+
+@pytest.mark.parametrize("name", SCENES)
+@pytest.mark.parametrize("watertight", [False, True])
+def test_trace_closest_bit_exact(ctx, loaded, name, watertight):
+    b, o = loaded(ctx, name)
+    rng = np.random.default_rng(42)
+    rays = scene_rays(b, 20000 if name != "instances" else 4000, rng)
+    flags = capi.BN_TRACE_WATERTIGHT if watertight else 0
+    g = ctx.trace(rays, flags)
+    h, _ = o.trace(rays, flags)
+    assert (h["instance"] >= 0).mean() > 0.3, "the ray set must hit the scene"
+    same_id = (g["instance"] == h["instance"]) & (g["primitive"] == h["primitive"])
+    assert same_id.all(), f"{(~same_id).sum()} closest-hit id mismatches of {len(rays)}"
+    hit = h["instance"] >= 0
+    for f in ("t", "u", "v"):
+        assert np.array_equal(g[f][hit].view(np.uint32), h[f][hit].view(np.uint32)), f"{f} not bit-exact"
+    np.testing.assert_allclose(g["normal"][hit], h["normal"][hit], rtol=0, atol=0)
+    np.testing.assert_allclose(g["position"][hit], h["position"][hit], rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_trace_any_matches_oracle(ctx, loaded, name):
+    b, o = loaded(ctx, name)
+    rng = np.random.default_rng(7)
+    rays = scene_rays(b, 20000 if name != "instances" else 4000, rng)
+    rays["t_max"] = rng.uniform(0.01, 2.0 if name != "instances" else 60.0, len(rays)).astype(np.float32)
+    g = ctx.trace(rays, capi.BN_TRACE_ANY)
+    h, _ = o.trace(rays, capi.BN_TRACE_ANY)
+    assert 0.05 < (h["instance"] >= 0).mean() < 0.95
+    assert np.array_equal(g["instance"] >= 0, h["instance"] >= 0)
+
+
+def test_watertight_and_moller_trumbore_agree_off_edges(ctx, loaded):
+    b, o = loaded(ctx, "cornell-objects")
+    rays = scene_rays(b, 50000, np.random.default_rng(3))
+    mt = ctx.trace(rays, 0)
+    wt = ctx.trace(rays, capi.BN_TRACE_WATERTIGHT)
+    same = (mt["instance"] == wt["instance"]) & (mt["primitive"] == wt["primitive"])
+    # the two tests differ only for rays through shared edges/vertices
+    assert same.mean() > 0.999
+    both = same & (mt["instance"] >= 0)
+    np.testing.assert_allclose(wt["t"][both], mt["t"][both], rtol=1e-5)
+
+
+def test_trace_counters(ctx, loaded):
+    b, o = loaded(ctx, "cornell-objects")
+    rays = scene_rays(b, 5000, np.random.default_rng(5))
+    ctx.reset_stats()
+    ctx.trace(rays, capi.BN_TRACE_COUNT)
+    s = ctx.stats()
+    _, counts = o.trace(rays, 0)
+    assert s.rays == counts[0] and s.nodes_visited == counts[1]
+    assert s.tris_tested == counts[2] and s.instances_visited == counts[3]
+
+
+def test_sampler_stream_bit_exact(ctx):
+    rng = np.random.default_rng(1)
+    seeds = rng.integers(0, 2**32, size=(4096, 3), dtype=np.uint64).astype(np.uint32)
+    g = ctx.sampler_stream(seeds, 32)
+    h = pyoracle.sampler_stream(seeds, 32)
+    assert g.tobytes() == h.tobytes()
+
+
+def bsdf_materials():
+    rng = np.random.default_rng(9)
+    mats = []
+    for t in range(4):
+        for _ in range(6):
+            c = (C.c_float * 3)(*rng.uniform(0.05, 0.95, 3))
+            mats.append(capi.bn_material_desc(t, c, float(rng.uniform(1.2, 2.0)), float(rng.uniform(0.05, 1.0)),
+                                              float(rng.choice([0.0, 1.0, rng.uniform()])), 0))
+    return mats
+
+
+def test_bsdf_eval_within_1e5_of_fp64_oracle(ctx):
+    b = Bundle.generate("cornell", 1)
+    mats = bsdf_materials()
+    # the materials go through a scene upload so the device tables hold them
+    s = b.scene.contents
+    arr = (capi.bn_material_desc * len(mats))(*mats)
+    s.materials = arr
+    s.n_materials = len(mats)
+    for i in range(s.n_instances):
+        if s.instances[i].material >= 0:
+            s.instances[i].material = 0
+    ctx.upload(b)
+    rng = np.random.default_rng(2)
+    n = 20000
+    q = np.zeros(n, capi.BSDF_QUERY_DTYPE)
+    q["material"] = rng.integers(0, len(mats), n)
+
+    def dirs(m):
+        d = rng.normal(size=(m, 3))
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        d[:, 2] = np.abs(d[:, 2]) * rng.choice([-1, 1], m)
+        return d.astype(np.float32)
+
+    q["wo"], q["wi"] = dirs(n), dirs(n)
+    # avoid grazing directions where |cos| < 0.05 (the relative bar is for well-posed values)
+    keep = (np.abs(q["wo"][:, 2]) > 0.05) & (np.abs(q["wi"][:, 2]) > 0.05)
+    q = q[keep]
+    g = ctx.bsdf(q, sample=False)
+    h = pyoracle.bsdf(mats, q, sample=False, use_double=True)
+    want = h[:, :4]
+    got = np.concatenate([g["bsdf"], g["pdf"][:, None]], 1).astype(np.float64)
+    scale = np.maximum(np.abs(want), 1e-30)
+    rel = np.abs(got - want) / scale
+    big = np.abs(want) > 1e-6 * np.abs(want).max(axis=0, keepdims=True)
+    assert np.percentile(rel[big], 100) < 1e-5, f"max rel err {rel[big].max():.3e}"
+    # sample: value and pdf at the sampled direction, against FP64 evaluation there
+    q["u_lobe"] = rng.uniform(0, 1, len(q)).astype(np.float32)
+    q["u_bsdf"] = rng.uniform(0, 0.999, (len(q), 2)).astype(np.float32)
+    gs = ctx.bsdf(q, sample=True)
+    hs = pyoracle.bsdf(mats, q, sample=True, use_double=True)
+    np.testing.assert_allclose(gs["wi"], hs[:, 4:7], atol=2e-5)
+    ok = np.isfinite(hs[:, 3]) & (np.abs(hs[:, 3]) > 1e-6)
+    np.testing.assert_allclose(gs["pdf"][ok], hs[ok, 3], rtol=2e-3)
+
+
+def test_device_error_word_reports_bad_material_index(ctx):
+    b = Bundle.generate("cornell", 1)
+    ctx.upload(b)
+    q = np.zeros(4, capi.BSDF_QUERY_DTYPE)
+    q["material"] = [0, 1, 99, 2]
+    q["wo"] = [0, 0, 1]
+    q["wi"] = [0, 0, 1]
+    with pytest.raises(BarnacleError) as e:
+        ctx.bsdf(q, sample=False)
+    assert e.value.code == capi.BN_ERR_DEVICE
+    assert ctx.stats().device_error & capi.BN_DEVERR_BAD_INDEX
+    # the context stays usable after the reported error
+    ctx.bsdf(q[:2], sample=False)
+
+
+def test_render_specular_scene_bit_identical(ctx):
+    """Mirrors and dielectrics only: no transcendental function on any path, so the device render
+    reproduces the oracle's floats exactly (1 spp: no cross-sample summation order)."""
+    b = Bundle.generate("cornell", 1)
+    s = b.scene.contents
+    for i in range(s.n_materials):
+        s.materials[i].type = capi.BN_MAT_MIRROR if i % 2 == 0 else capi.BN_MAT_DIELECTRIC
+    ctx.upload(b)
+    o = pyoracle.Scene(b.scene)
+    r = b.render
+    r.spp = 1
+    v = b.views[0]
+    img = ctx.render(r, v)[0]
+    ref, _ = o.render_pt(r, v)
+    assert img.max() > 1.0, "the light must be visible"
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), \
+        f"{(img != ref).any(axis=2).sum()} pixels differ"
+
+
+def pixel_stats(frames):
+    f = np.stack(frames).astype(np.float64)
+    return f.mean(0), f.std(0, ddof=1) / np.sqrt(len(frames))
+
+
+@pytest.mark.parametrize("name,crop,spp,frames", [("cornell", (96, 96, 160, 160), 16, 12),
+                                                   ("cornell-objects", (200, 200, 264, 264), 8, 12)])
+def test_render_megakernel_statistically_matches_oracle(ctx, loaded, name, crop, spp, frames):
+    b, o = loaded(ctx, name)
+    r = b.render
+    r.spp = spp
+    v = b.views[0]
+    x0, y0, x1, y1 = crop
+    gpu, cpu = [], []
+    for f in range(frames):
+        r.frame_id = f
+        gpu.append(ctx.render(r, v)[0])
+        r.frame_id = 1000 + f
+        img, _ = o.render_pt(r, v, crop=crop)
+        cpu.append(img)
+    H = v.height
+    rows = slice(H - y1, H - y0)  # Film.Pixels rows are flipped
+    cols = slice(x0, x1)
+    mg, sg = pixel_stats([g[rows, cols] for g in gpu])
+    mc, sc = pixel_stats([c[rows, cols] for c in cpu])
+    se = np.sqrt(sg ** 2 + sc ** 2)
+    z = np.abs(mg - mc) / np.maximum(se, 1e-12)
+    valid = se > 0
+    frac = (z[valid] > 3).mean()
+    assert frac < 0.02, f"{frac:.3%} of pixel means differ by more than 3 standard errors"
+    # RMSE at equal spp: each estimator against the other's mean (same noise level expected)
+    rg = np.sqrt(((np.stack([g[rows, cols] for g in gpu]) - mc) ** 2).mean())
+    rc = np.sqrt(((np.stack([c[rows, cols] for c in cpu]) - mg) ** 2).mean())
+    assert abs(rg / rc - 1) < 0.1
+
+
+def test_render_api_errors(ctx):
+    b = Bundle.generate("cornell", 1)
+    ctx.upload(b)
+    r = b.render
+    r.spp = 0
+    with pytest.raises(BarnacleError) as e:
+        ctx.render(r, b.views[0])
+    assert e.value.code == capi.BN_ERR_INVALID_ARG
+    v = b.views[0]
+    v.width = 0
+    r.spp = 1
+    with pytest.raises(BarnacleError):
+        ctx.render(r, v)
+
+
+def test_no_scene_and_bad_scene_errors():
+    from barnacle_gb300 import Context
+    with Context(0) as c:
+        with pytest.raises(BarnacleError) as e:
+            c.trace(random_rays(4, np.zeros(3), np.ones(3), np.random.default_rng(0)))
+        assert e.value.code == capi.BN_ERR_NO_SCENE
+        b = Bundle.generate("cornell", 1)
+        s = b.scene.contents
+        s.instances[0].material = 77
+        with pytest.raises(BarnacleError) as e:
+            c.upload(b)
+        assert e.value.code == capi.BN_ERR_INVALID_ARG
+        s.instances[0].material = 0
+        for i in range(s.n_instances):
+            s.instances[i].light = -1
+        with pytest.raises(BarnacleError, match="No light primitives"):
+            c.upload(b)

@@ -1,0 +1,299 @@
+"""CPU tests: the oracle against the golden vectors, the library's host preparation against the
+oracle (bit-exact BVH builds), the scene generators and loaders, and the C-ABI symbol table."""
+import json
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from barnacle_gb300 import Bundle, BarnacleError, bvh_build, capi, mat4_invert
+from oracle import pyoracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def load(name):
+    return json.loads((GOLDEN / f"{name}.json").read_text())
+
+
+# ------------------------------------------------------------------ sampler (Util/Hash.fs)
+def test_oracle_hash_and_lcg_match_golden():
+    g = load("sampler")
+    L = pyoracle.lib()
+    for case in g["three"]:
+        assert L.or_xxhash32_three(*case["seed"]) == case["hash"]
+    for case in g["two"]:
+        assert L.or_xxhash32_two(*case["xy"]) == case["hash"]
+    seeds = np.array([c["seed"] for c in g["three"]], np.uint32)
+    draws = pyoracle.sampler_stream(seeds, 16)
+    want = np.array([c["draws"] for c in g["three"]], np.float32)
+    assert draws.tobytes() == want.tobytes()
+
+
+# ------------------------------------------------------------------ BVH builder (Util/BVH.fs)
+def nodes_tuple(nodes):
+    return [(list(map(float, n["bounds_min"])), list(map(float, n["bounds_max"])), int(n["right_or_offset"]),
+             int(n["is_leaf"]), int(n["split_axis"]) if not n["is_leaf"] else 0,
+             int(n["count"]) if n["is_leaf"] else 0) for n in nodes]
+
+
+@pytest.mark.parametrize("case_index", range(9))
+def test_bvh_oracle_and_library_match_golden(case_index):
+    case = load("bvh")[case_index]
+    boxes = np.array(case["boxes"], np.float32)
+    want = [(n[0], n[1], n[2], n[3], n[4], n[5]) for n in case["nodes"]]
+    on, op = pyoracle.bvh_build(boxes)
+    ln, lp = bvh_build(boxes)
+    assert nodes_tuple(on) == want, f"oracle differs from golden ({case['kind']})"
+    assert list(op) == case["perm"]
+    assert nodes_tuple(ln) == want, f"library differs from golden ({case['kind']})"
+    assert list(lp) == case["perm"]
+
+
+def test_bvh_empty_and_single():
+    n, p = bvh_build(np.zeros((0, 6), np.float32))
+    assert len(n) == 1 and n[0]["is_leaf"] == 1 and n[0]["count"] == 0
+    n, p = bvh_build(np.array([[0, 0, 0, 1, 1, 1]], np.float32))
+    assert len(n) == 1 and n[0]["count"] == 1 and list(p) == [0]
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_bvh_library_matches_oracle_random_large(seed):
+    rng = np.random.default_rng(seed)
+    n = 5000
+    c = rng.uniform(-100, 100, size=(n, 3))
+    # clusters and duplicates exercise the zero-extent median split
+    c[: n // 10] = c[0]
+    e = rng.exponential(1.0, size=(n, 3))
+    boxes = np.concatenate([c - e, c + e], 1).astype(np.float32)
+    on, op = pyoracle.bvh_build(boxes)
+    ln, lp = bvh_build(boxes)
+    assert on.tobytes() == ln.tobytes()
+    assert np.array_equal(op, lp)
+
+
+@pytest.mark.parametrize("name", ["cornell", "cornell-objects", "instances"])
+def test_scene_blas_and_tlas_library_match_oracle(name):
+    b = Bundle.generate(name, 1)
+    s = b.scene.contents
+    osc = pyoracle.Scene(b.scene)
+    for mi in range(s.n_meshes):
+        m = s.meshes[mi]
+        nt = m.n_triangles
+        V = np.ctypeslib.as_array(m.vertices, shape=(m.n_vertices * 3,)).reshape(-1, 3)
+        I = np.ctypeslib.as_array(m.indices, shape=(nt * 3,)).reshape(-1, 3)
+        P = V[I]
+        # Triangle.Bounds = MinNative/MaxNative of the vertices (no NaNs here, so min/max agree)
+        boxes = np.concatenate([P.min(1), P.max(1)], 1).astype(np.float32)
+        ln, lp = bvh_build(boxes)
+        on, op = osc.blas(mi, nt)
+        assert ln.tobytes() == on.tobytes(), f"{name}: BLAS of mesh {mi} differs"
+        assert np.array_equal(lp, op)
+
+
+# ------------------------------------------------------------------ triangle test (Mesh.fs)
+def one_triangle_desc(tri, keep):
+    import ctypes as C
+    v = np.ascontiguousarray(np.array(tri, np.float32).reshape(-1))
+    idx = np.array([0, 1, 2], np.int32)
+    mesh = capi.bn_mesh_desc(v.ctypes.data_as(C.POINTER(C.c_float)), idx.ctypes.data_as(C.POINTER(C.c_int32)), None, 3, 1)
+    prims = (capi.bn_primitive_desc * 1)(capi.bn_primitive_desc(0, 0, 0.0))
+    meshes = (capi.bn_mesh_desc * 1)(mesh)
+    eye = (C.c_float * 16)(*np.eye(4, dtype=np.float32).reshape(-1))
+    inst = capi.bn_instance_desc(0, 0, 0, 0, eye, eye)
+    insts = (capi.bn_instance_desc * 1)(inst)
+    mats = (capi.bn_material_desc * 1)(capi.bn_material_desc(0, (C.c_float * 3)(1, 1, 1), 1.5, 1.0, 0.0, 0.0))
+    lights = (capi.bn_light_desc * 1)(capi.bn_light_desc((C.c_float * 3)(1, 1, 1), 1))
+    d = capi.bn_scene_desc(prims, 1, meshes, 1, insts, 1, mats, 1, lights, 1, 0)
+    keep += [v, idx, mesh, prims, meshes, insts, mats, lights, d]
+    return C.pointer(d)
+
+
+def test_oracle_triangle_intersection_matches_golden():
+    g = load("triangle")
+    keep = []
+    desc = one_triangle_desc(g["triangle"], keep)
+    osc = pyoracle.Scene(desc)
+    rays = np.zeros(len(g["rays"]), capi.RAY_DTYPE)
+    for i, r in enumerate(g["rays"]):
+        rays[i]["origin"] = r["o"]
+        rays[i]["direction"] = r["d"]
+        rays[i]["t_max"] = np.inf
+    hits, _ = osc.trace(rays)
+    n_hit = 0
+    for i, r in enumerate(g["rays"]):
+        if r["hit"] is None:
+            assert hits[i]["instance"] == -1, f"ray {i}: oracle hit, golden missed"
+        else:
+            n_hit += 1
+            assert hits[i]["instance"] == 0, f"ray {i}: oracle missed, golden hit"
+            t, u, v = r["hit"]
+            assert np.float32(hits[i]["t"]) == np.float32(t)
+            assert np.float32(hits[i]["u"]) == np.float32(u)
+            assert np.float32(hits[i]["v"]) == np.float32(v)
+    assert n_hit > 10
+
+
+# ------------------------------------------------------------------ BSDFs in FP64
+def bsdf_queries(g):
+    q = np.zeros(len(g["cases"]), capi.BSDF_QUERY_DTYPE)
+    for i, c in enumerate(g["cases"]):
+        q[i]["material"] = c["material"]
+        q[i]["wo"] = c["wo"]
+        q[i]["wi"] = c["wi"]
+    return q
+
+
+def golden_materials(g):
+    import ctypes as C
+    return [capi.bn_material_desc(m["type"], (C.c_float * 3)(*m["base"]), m["ior"], m["roughness"], m["metallic"], 0)
+            for m in g["materials"]]
+
+
+def test_oracle_bsdf_eval_fp64_and_fp32_match_golden():
+    g = load("bsdf")
+    q = bsdf_queries(g)
+    mats = golden_materials(g)
+    o64 = pyoracle.bsdf(mats, q, sample=False, use_double=True)
+    o32 = pyoracle.bsdf(mats, q, sample=False, use_double=False)
+    want = np.array([c["bsdf"] + [c["pdf"]] for c in g["cases"]])
+    np.testing.assert_allclose(o64[:, :4], want, rtol=1e-6, atol=1e-12)
+    # the FP32 restatement keeps the reference's GGX D = a^2 / (pi (1 + (a^2 - 1) c^2)^2), whose
+    # cancellation costs ~eps/a^2 relative for sharp lobes (a = 0.04 here): 1e-4, not 1e-5
+    np.testing.assert_allclose(o32[:, :4], want, rtol=1e-4, atol=1e-7)
+
+
+# ------------------------------------------------------------------ scenes and loaders
+def test_generated_workloads_have_the_stated_sizes():
+    c0 = Bundle.generate("cornell")
+    assert c0.n_triangles_instanced == 36
+    v = c0.views[0]
+    assert (v.width, v.height) == (256, 256) and c0.render.spp == 64 and c0.render.max_depth == 8
+    c1 = Bundle.generate("cornell-objects")
+    assert c1.n_triangles_instanced == 36 + 81920 + 20480 + 2
+    assert c1.render.spp == 256 and c1.render.max_depth == 16
+    c2 = Bundle.generate("instances")
+    assert c2.scene.contents.n_instances == 1 + 1024 + 64
+    assert len(c2.views) == 16
+    assert 140_000_000 < c2.n_triangles_instanced < 180_000_000
+    pix = [(v.width, v.height) for v in c2.views]
+    assert min(w * h for w, h in pix) >= 256 * 240 and max(w * h for w, h in pix) <= 1920 * 1080
+    c3 = Bundle.generate("pssmlt")
+    r = c3.render
+    assert r.integrator == capi.BN_INTEGRATOR_PSSMLT and r.n_chains == 65536 and r.n_bootstrap == 1 << 20
+    assert abs(r.large_step_prob - 0.3) < 1e-7 and r.mutation == capi.BN_MUTATION_KELEMEN
+    assert abs(r.eps_max - 1 / 64) < 1e-9 and c3.views[0].width == 1024
+    c4 = Bundle.generate("materials")
+    assert c4.n_slots == 32 and c4.emissive_slot_base == 28 and len(c4.slot_params()) == 32 * 6
+
+
+def test_generation_is_deterministic():
+    a = Bundle.generate("instances", 3)
+    b = Bundle.generate("instances", 3)
+    sa, sb = a.scene.contents, b.scene.contents
+    for i in range(sa.n_instances):
+        assert bytes(sa.instances[i]) == bytes(sb.instances[i])
+    m = sa.meshes[3]
+    va = np.ctypeslib.as_array(m.vertices, shape=(m.n_vertices * 3,))
+    vb = np.ctypeslib.as_array(sb.meshes[3].vertices, shape=(m.n_vertices * 3,))
+    assert va.tobytes() == vb.tobytes()
+
+
+def test_geodesic_meshes_are_closed():
+    c2 = Bundle.generate("instances")
+    s = c2.scene.contents
+    for mi in range(4):
+        m = s.meshes[mi]
+        I = np.ctypeslib.as_array(m.indices, shape=(m.n_triangles * 3,)).reshape(-1, 3)
+        e = np.sort(np.concatenate([I[:, [0, 1]], I[:, [1, 2]], I[:, [2, 0]]]), axis=1)
+        _, counts = np.unique(e, axis=0, return_counts=True)
+        assert np.all(counts == 2), "every edge of a closed mesh is shared by exactly two triangles"
+        assert m.n_vertices == m.n_triangles // 2 + 2  # Euler characteristic 2
+
+
+def test_json_loader_reference_schema(tmp_path):
+    scene = GOLDEN / "scenes" / "spheres_thinlens.json"
+    b = Bundle.load_json(str(scene))
+    s = b.scene.contents
+    assert s.n_primitives == 5 and s.n_instances == 7
+    r = b.render
+    assert r.integrator == capi.BN_INTEGRATOR_PSSMLT and r.spp == 4 and r.max_depth == 6
+    assert r.mutation == capi.BN_MUTATION_KELEMEN and abs(r.eps_max - 1 / 16) < 1e-9
+    v = b.views[0]
+    assert v.camera.type == capi.BN_CAM_THIN_LENS and v.width == 96 and v.height == 72
+    assert abs(v.camera.aperture - 0.5) < 1e-7 and abs(v.camera.push_forward - 10) < 1e-6
+    # camera node translation (50, 40.8, 295.6); rotations are radians
+    assert np.allclose(list(v.camera.camera_to_world)[12:15], [50, 40.8, 295.6], atol=1e-4)
+    # the instance under two nodes is listed twice with the last traversal's transform
+    prims = [s.instances[i].primitive for i in range(s.n_instances)]
+    assert prims.count(4) == 2
+    twice = [i for i in range(s.n_instances) if s.instances[i].primitive == 4]
+    assert list(s.instances[twice[0]].object_to_world) == list(s.instances[twice[1]].object_to_world)
+    # defaults: albedo 1, roughness 1, metallic 0, ior 1.5; two-sided default true
+    m = s.materials[3]
+    assert list(m.base_color) == [1, 1, 1] and m.roughness == 1 and m.metallic == 0 and abs(m.ior - 1.5) < 1e-7
+    assert s.lights[0].two_sided == 1
+
+
+def test_json_loader_errors(tmp_path):
+    p = tmp_path / "bad.json"
+    p.write_text('{"nodes": [{}], "integrator": {"type": "nope"}, "camera": {"type": "pinhole"}, '
+                 '"film": {"width": 4, "height": 4, "tone-mapping": "aces"}}')
+    with pytest.raises(BarnacleError, match="Unknown integrator type"):
+        Bundle.load_json(str(p))
+    p.write_text("{ not json")
+    with pytest.raises(BarnacleError):
+        Bundle.load_json(str(p))
+    with pytest.raises(BarnacleError):
+        Bundle.load_json(str(tmp_path / "missing.json"))
+    with pytest.raises(BarnacleError, match="unknown workload"):
+        Bundle.generate("no-such-workload")
+
+
+@pytest.mark.skipif(not Path("/root/reference/Asset/cbox.json").exists(), reason="reference asset not mounted")
+def test_json_loader_reads_reference_cbox():
+    b = Bundle.load_json("/root/reference/Asset/cbox.json")
+    s = b.scene.contents
+    assert s.n_instances == 9 and s.n_primitives == 9
+    assert b.render.integrator == capi.BN_INTEGRATOR_PSSMLT and b.render.spp == 16
+    assert b.views[0].width == 1024 and b.views[0].height == 768
+
+
+def test_obj_loader_fan_triangulation_and_negative_indices(tmp_path):
+    obj = tmp_path / "m.obj"
+    obj.write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3 4\nf -4/1 -2/2 -1/3\n")
+    scene = tmp_path / "s.json"
+    scene.write_text(json.dumps({
+        "nodes": [{"instances": [0], "children": [1]}, {"has-camera": True}],
+        "instances": [{"primitive": 0, "light": 0}],
+        "primitives": [{"type": "mesh", "uri": str(obj)}],
+        "lights": [{"type": "diffuse", "emission": [1, 1, 1]}],
+        "integrator": {"type": "path-tracing"}, "camera": {"type": "pinhole"},
+        "film": {"width": 8, "height": 8, "tone-mapping": "identity"}}))
+    b = Bundle.load_json(str(scene))
+    m = b.scene.contents.meshes[0]
+    idx = np.ctypeslib.as_array(m.indices, shape=(m.n_triangles * 3,)).tolist()
+    assert idx == [0, 1, 2, 0, 2, 3, 0, 2, 3]
+
+
+def test_mat4_invert():
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        m = rng.normal(size=(4, 4)).astype(np.float32)
+        m[:, 3] = [0, 0, 0, 1]
+        inv = mat4_invert(m).reshape(4, 4)
+        np.testing.assert_allclose(m.astype(np.float64) @ inv, np.eye(4), atol=1e-4)
+
+
+# ------------------------------------------------------------------ the C-ABI surface
+def test_library_exports_every_declared_symbol():
+    header = (ROOT / "include" / "barnacle_gpu.h").read_text()
+    declared = set(re.findall(r"^(?:int|const char\*|void)\s+(bn_[a-z0-9_]+)\s*\(", header, flags=re.M))
+    assert len(declared) >= 20
+    lib = capi.load_library()
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert not missing, f"declared but not exported: {missing}"
+    assert declared <= set(capi.SIGNATURES), "every declared entry point has a ctypes signature"
+    assert lib.bn_version().decode().startswith("barnacle-gb300")
