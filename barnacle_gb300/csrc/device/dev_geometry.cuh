@@ -309,14 +309,11 @@ __device__ __forceinline__ bool trace_closest(const DevScene& s, const Ray& ray,
           if (kCount) cnt->tris++;
           const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
           float tt, uu, vv;
-          bool h;
-          if (kWatertight) {
-            h = tri_wt(p0, p1, p2, oray, wt, t, &tt, &uu, &vv);
-          } else {
-            // the triangle's own AABB pre-test (Mesh.fs:231), then Moller-Trumbore
-            const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
-            h = box_hit(lo, hi, oray, oinv, t) && tri_mt(p0, p1, p2, oray, t, &tt, &uu, &vv);
-          }
+          // the triangle's own AABB pre-test (Mesh.fs:231; its 1e-3 near bound is part of the
+          // reference's self-intersection behaviour), then the triangle test
+          const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
+          bool h = box_hit(lo, hi, oray, oinv, t);
+          if (h) h = kWatertight ? tri_wt(p0, p1, p2, oray, wt, t, &tt, &uu, &vv) : tri_mt(p0, p1, p2, oray, t, &tt, &uu, &vv);
           if (h) {
             t = tt; found = true;
             hit->inst = k; hit->tri = j; hit->t = tt; hit->u = uu; hit->v = vv; hit->sphere_root = 0;
@@ -385,13 +382,9 @@ __device__ __forceinline__ bool trace_any(const DevScene& s, const Ray& ray, flo
           if (kCount) cnt->tris++;
           const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
           float tt, uu, vv;
-          bool h;
-          if (kWatertight) {
-            h = tri_wt(p0, p1, p2, oray, wt, tmax, &tt, &uu, &vv);
-          } else {
-            const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
-            h = box_hit(lo, hi, oray, oinv, tmax) && tri_mt(p0, p1, p2, oray, tmax, &tt, &uu, &vv);
-          }
+          const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
+          bool h = box_hit(lo, hi, oray, oinv, tmax);
+          if (h) h = kWatertight ? tri_wt(p0, p1, p2, oray, wt, tmax, &tt, &uu, &vv) : tri_mt(p0, p1, p2, oray, tmax, &tt, &uu, &vv);
           if (h) return true;
         }
       }

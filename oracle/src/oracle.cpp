@@ -428,9 +428,9 @@ struct Mesh {
         for (int k = node.right_or_offset; k < node.right_or_offset + node.count; ++k) {
           const Triangle tr = Tri(k);
           c->tris++;
-          bool h;
-          if (wt) h = tr.IntersectWatertight(ray, t, u, v);
-          else h = BoxIntersect(tr.Bounds(), ray, *t) && tr.Intersect(ray, t, u, v);
+          // the triangle AABB pre-test (Mesh.fs:231) precedes either triangle test
+          bool h = BoxIntersect(tr.Bounds(), ray, *t);
+          if (h) h = wt ? tr.IntersectWatertight(ray, t, u, v) : tr.Intersect(ray, t, u, v);
           if (h) { *tag = k; hit = true; }
         }
       } else if (ray.Direction[node.split_axis] > 0.f) {
@@ -458,9 +458,8 @@ struct Mesh {
           const Triangle tr = Tri(k);
           c->tris++;
           float tt = t, u, v;
-          bool h;
-          if (wt) h = tr.IntersectWatertight(ray, &tt, &u, &v);
-          else h = BoxIntersect(tr.Bounds(), ray, t) && tr.Intersect(ray, &tt, &u, &v);
+          bool h = BoxIntersect(tr.Bounds(), ray, t);
+          if (h) h = wt ? tr.IntersectWatertight(ray, &tt, &u, &v) : tr.Intersect(ray, &tt, &u, &v);
           if (h) return true;
         }
       } else if (ray.Direction[node.split_axis] > 0.f) {

@@ -113,10 +113,15 @@ def test_watertight_and_moller_trumbore_agree_off_edges(ctx, loaded):
     mt = ctx.trace(rays, 0)
     wt = ctx.trace(rays, capi.BN_TRACE_WATERTIGHT)
     same = (mt["instance"] == wt["instance"]) & (mt["primitive"] == wt["primitive"])
-    # the two tests differ only for rays through shared edges/vertices
-    assert same.mean() > 0.999
+    # Both paths share the reference's node and triangle AABB tests, so they differ only where
+    # the triangle tests themselves do: rays through shared edges/vertices (adjacent triangle
+    # picked) and hits a hair from the ray origin, where the two formulas round t differently.
+    far = (mt["t"] > 1e-2) & (wt["t"] > 1e-2)
+    assert same[far].mean() > 0.9995, f"id mismatch rate {1 - same[far].mean():.2e}"
     both = same & (mt["instance"] >= 0)
     np.testing.assert_allclose(wt["t"][both], mt["t"][both], rtol=1e-5)
+    both_hit = (mt["instance"] >= 0) & (wt["instance"] >= 0) & far
+    np.testing.assert_allclose(wt["t"][both_hit], mt["t"][both_hit], rtol=1e-5)
 
 
 def test_trace_counters(ctx, loaded):
@@ -184,14 +189,27 @@ def test_bsdf_eval_within_1e5_of_fp64_oracle(ctx):
     rel = np.abs(got - want) / scale
     big = np.abs(want) > 1e-6 * np.abs(want).max(axis=0, keepdims=True)
     assert np.percentile(rel[big], 100) < 1e-5, f"max rel err {rel[big].max():.3e}"
-    # sample: value and pdf at the sampled direction, against FP64 evaluation there
+    # sample: the sampled direction against the FP64 sampler (sin/cos/atan differ by ulps), and
+    # the returned value and pdf against an FP64 evaluation AT the device's sampled direction
+    # (a sharp GGX lobe turns 1e-7 of direction noise into percent-level pdf changes)
     q["u_lobe"] = rng.uniform(0, 1, len(q)).astype(np.float32)
     q["u_bsdf"] = rng.uniform(0, 0.999, (len(q), 2)).astype(np.float32)
     gs = ctx.bsdf(q, sample=True)
     hs = pyoracle.bsdf(mats, q, sample=True, use_double=True)
     np.testing.assert_allclose(gs["wi"], hs[:, 4:7], atol=2e-5)
-    ok = np.isfinite(hs[:, 3]) & (np.abs(hs[:, 3]) > 1e-6)
-    np.testing.assert_allclose(gs["pdf"][ok], hs[ok, 3], rtol=2e-3)
+    types = np.array([mats[m].type for m in q["material"]])
+    delta = (types == capi.BN_MAT_MIRROR) | (types == capi.BN_MAT_DIELECTRIC)
+    np.testing.assert_allclose(gs["pdf"][delta], hs[delta, 3], rtol=1e-6)
+    np.testing.assert_allclose(gs["bsdf"][delta], hs[delta, :3], rtol=1e-6)
+    qe = q.copy()
+    qe["wi"] = gs["wi"]
+    he = pyoracle.bsdf(mats, qe, sample=False, use_double=True)
+    smooth = ~delta & (np.abs(gs["wi"][:, 2]) > 1e-3) & (np.abs(he[:, 3]) > 1e-6)
+    got = np.concatenate([gs["bsdf"], gs["pdf"][:, None]], 1)[smooth].astype(np.float64)
+    want = he[smooth, :4]
+    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-30)
+    big = np.abs(want) > 1e-6 * np.abs(want).max(axis=0, keepdims=True)
+    assert rel[big].max() < 1e-5, f"max rel err {rel[big].max():.3e}"
 
 
 def test_device_error_word_reports_bad_material_index(ctx):
