@@ -159,6 +159,7 @@ SIGNATURES = {
     "bn_sampler_stream": (C.c_int, [P, P, C.c_int64, C.c_int32, P]),
     "bn_render": (C.c_int, [P, C.POINTER(bn_render_desc), C.POINTER(bn_view), C.c_int32, P]),
     "bn_film_download": (C.c_int, [P, P, C.c_int64]),
+    "bn_render_noalloc": (C.c_int, [P, C.POINTER(bn_render_desc), C.POINTER(bn_view), C.c_int32, P]),
     "bn_get_stats": (C.c_int, [P, C.POINTER(bn_stats)]),
     "bn_reset_stats": (C.c_int, [P]),
     "bn_forward": (C.c_int, [P, C.POINTER(bn_adjoint_desc), P, P, P]),

@@ -246,6 +246,21 @@ int bn_sampler_stream(bn_context* ctx, const uint32_t* seeds, int64_t n_streams,
 int bn_render(bn_context* ctx, const bn_render_desc* desc, const bn_view* views, int32_t n_views,
               float* out_rgb);
 int bn_film_download(bn_context* ctx, float* out_rgb, int64_t n_floats);
+
+/* Render without allocating device memory (no counterpart in the reference).
+ * For callers that cannot allocate during a render: a host whose device memory all comes from
+ * its own arena and whose frame loop must not call cudaMalloc/cudaFree (they synchronise the
+ * device), or a caller with a fixed memory budget on a shared GPU.  Same images as bn_render in
+ * megakernel mode (integrator BN_INTEGRATOR_PATH, mode BN_MODE_MEGAKERNEL only), written to
+ * film_device, a caller-owned DEVICE buffer of width*height*3 floats per view, views back to back
+ * in Film.Pixels order.  The scene must already be uploaded (bn_scene_upload allocates; do it at
+ * set-up time).  Scratch lives in one static device array of the library: 64 view records and
+ * 1,048,576 partial sums (16 MiB), held by every GPU that loads the library until exit.  Limits:
+ * at most 64 views and 1,048,576 pixels in total; larger renders return BN_ERR_INVALID_ARG.  The
+ * first call on a device resolves the array's address (set-up): make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race. */
+int bn_render_noalloc(bn_context* ctx, const bn_render_desc* desc, const bn_view* views, int32_t n_views,
+                      float* film_device);
 int bn_get_stats(const bn_context* ctx, bn_stats* out);
 int bn_reset_stats(bn_context* ctx);
 
