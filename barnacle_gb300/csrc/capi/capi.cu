@@ -154,6 +154,7 @@ int bn_destroy(bn_context* ctx) {
                     &ctx->mlt_boot, &ctx->mlt_chain, &ctx->adj_params, &ctx->adj_image, &ctx->adj_target,
                     &ctx->adj_grad, &ctx->adj_aux};
   for (DevBuf* b : bufs) b->release();
+  if (ctx->wf && ctx->wf_release) ctx->wf_release(ctx->wf);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   cudaEventDestroy(ctx->ev2);

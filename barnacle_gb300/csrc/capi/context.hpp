@@ -57,6 +57,11 @@ struct bn_context {
   // pssmlt / adjoint scratch
   DevBuf mlt_state, mlt_boot, mlt_chain, adj_params, adj_image, adj_target, adj_grad, adj_aux;
 
+  // wavefront path state, captured graph and tuned launch shape (owned by wavefront.cu)
+  void* wf = nullptr;
+  void (*wf_release)(void*) = nullptr;
+  long long scene_generation = 0;  // bumped by every bn_scene_upload
+
   int fail(int code, const std::string& msg) {
     err = msg;
     return code;

@@ -337,6 +337,7 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   ctx->host_mats = mats;
   ctx->host_inst_light = inst_light;
   ctx->n_lights = d->n_lights;
+  ctx->scene_generation += 1;
   ctx->has_scene = true;
   return BN_OK;
 }

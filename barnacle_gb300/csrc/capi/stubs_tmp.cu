@@ -1,6 +1,5 @@
 #include "context.hpp"
 namespace bnc {
-int render_wavefront(bn_context* ctx, const bn_render_desc*, const std::vector<bn::DevView>&) { return ctx->fail(BN_ERR_UNSUPPORTED, "wavefront not built"); }
 int render_pssmlt(bn_context* ctx, const bn_render_desc*, const std::vector<bn::DevView>&) { return ctx->fail(BN_ERR_UNSUPPORTED, "pssmlt not built"); }
 }
 extern "C" int bn_forward(bn_context* ctx, const bn_adjoint_desc*, const float*, const float*, float*) { return ctx ? ctx->fail(BN_ERR_UNSUPPORTED, "adjoint not built") : BN_ERR_INVALID_ARG; }

@@ -1,0 +1,242 @@
+// Wavefront render orchestration: path-state buffers, the CUDA graph whose while-node runs the
+// whole bounce loop on the device, the host-driven fallback loop, and the launch autotuner.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../device/wavefront.hpp"
+#include "context.hpp"
+
+namespace {
+
+struct WfState {
+  int pool = 0;
+  DevBuf params, ray_o, ray_d, beta, L, meta, hit_f, hit_i, q_active, q_bins, shadow, counters, work_next, film_acc;
+  // captured graph (one per launch shape)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle cond = 0;
+  bool graph_failed = false;
+  bn::WfLaunch shape{};
+  int shape_cap = -1;
+  // autotuned choice per uploaded scene
+  long long tuned_generation = -1;
+  bool tuned_watertight = false;
+  int tuned_pool = 0, tuned_cap = 0;
+
+  void release() {
+    DevBuf* b[] = {&params, &ray_o, &ray_d, &beta, &L, &meta, &hit_f, &hit_i, &q_active, &q_bins, &shadow, &counters,
+                   &work_next, &film_acc};
+    for (DevBuf* x : b) x->release();
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
+WfState* state(bn_context* ctx) {
+  if (!ctx->wf) {
+    ctx->wf = new WfState();
+    ctx->wf_release = [](void* p) {
+      auto* s = static_cast<WfState*>(p);
+      s->release();
+      delete s;
+    };
+  }
+  return static_cast<WfState*>(ctx->wf);
+}
+
+cudaError_t ensure_pool(WfState* w, int pool) {
+  if (w->pool == pool) return cudaSuccess;
+  cudaError_t e;
+  const size_t P = static_cast<size_t>(pool);
+  if ((e = w->params.reserve(sizeof(bn::WfParams))) != cudaSuccess) return e;
+  if ((e = w->ray_o.reserve(P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->ray_d.reserve(P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->beta.reserve(P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->L.reserve(P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->meta.reserve(P * sizeof(int4))) != cudaSuccess) return e;
+  if ((e = w->hit_f.reserve(P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->hit_i.reserve(P * sizeof(int2))) != cudaSuccess) return e;
+  if ((e = w->q_active.reserve(P * sizeof(int))) != cudaSuccess) return e;
+  if ((e = w->q_bins.reserve(P * bn::kNumBins * sizeof(int))) != cudaSuccess) return e;
+  if ((e = w->shadow.reserve(P * 4 * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->counters.reserve(bn::kCntSize * sizeof(int))) != cudaSuccess) return e;
+  if ((e = w->work_next.reserve(sizeof(unsigned long long))) != cudaSuccess) return e;
+  w->pool = pool;
+  return cudaSuccess;
+}
+
+// the while-node graph: body = one iteration (regen, extend, shade, shadow, control)
+int build_graph(bn_context* ctx, WfState* w) {
+  if (w->exec) {
+    cudaGraphExecDestroy(w->exec);
+    w->exec = nullptr;
+  }
+  if (w->graph) {
+    cudaGraphDestroy(w->graph);
+    w->graph = nullptr;
+  }
+  cudaError_t e;
+  if ((e = cudaGraphCreate(&w->graph, 0)) != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphCreate");
+  if ((e = cudaGraphConditionalHandleCreate(&w->cond, w->graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+    return ctx->cuda_fail(e, "cudaGraphConditionalHandleCreate");
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = w->cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if ((e = cudaGraphAddNode(&node, w->graph, nullptr, nullptr, 0, &np)) != cudaSuccess)
+    return ctx->cuda_fail(e, "cudaGraphAddNode(while)");
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  if ((e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
+      cudaSuccess)
+    return ctx->cuda_fail(e, "cudaStreamBeginCaptureToGraph");
+  cudaError_t le = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, true, ctx->stream);
+  cudaGraph_t captured = body;
+  e = cudaStreamEndCapture(ctx->stream, &captured);
+  if (le != cudaSuccess) return ctx->cuda_fail(le, "capture of the bounce loop");
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaStreamEndCapture");
+  if ((e = cudaGraphInstantiate(&w->exec, w->graph, 0)) != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphInstantiate");
+  return BN_OK;
+}
+
+// One render (or a truncated tuning render) into w->film_acc / ctx->film.
+int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels, long long total_paths, int n_views,
+        int pool, int cap, bool use_graph, float* ms_out) {
+  cudaError_t e;
+  if ((e = ensure_pool(w, pool)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront path-state allocation");
+  if ((e = w->film_acc.reserve(static_cast<size_t>(n_pixels) * 3 * sizeof(double))) != cudaSuccess)
+    return ctx->cuda_fail(e, "wavefront film allocation");
+  const bool wt = d->flags & BN_RENDER_WATERTIGHT;
+  if (w->shape_cap != cap || w->shape.watertight != wt) {
+    w->shape = bn::wf_launch_shape(wt, cap);
+    w->shape_cap = cap;
+    if (w->exec) {
+      cudaGraphExecDestroy(w->exec);
+      w->exec = nullptr;
+    }
+  }
+  bn::WfParams p{};
+  p.scene = ctx->scene;
+  p.views = ctx->views.as<bn::DevView>();
+  p.n_views = n_views;
+  p.spp = d->spp;
+  p.max_depth = d->max_depth;
+  p.rr_depth = d->rr_depth;
+  p.frame_id = d->frame_id;
+  p.pool = pool;
+  p.total_paths = total_paths;
+  p.n_pixels = n_pixels;
+  p.max_iters = static_cast<int>(std::min<long long>(1LL << 30, (total_paths / pool + 2) * (d->max_depth + 2) + 64));
+  p.ray_o = w->ray_o.as<float4>();
+  p.ray_d = w->ray_d.as<float4>();
+  p.beta = w->beta.as<float4>();
+  p.L = w->L.as<float4>();
+  p.meta = w->meta.as<int4>();
+  p.hit_f = w->hit_f.as<float4>();
+  p.hit_i = w->hit_i.as<int2>();
+  p.q_active = w->q_active.as<int>();
+  p.q_bins = w->q_bins.as<int>();
+  p.shadow = w->shadow.as<float4>();
+  p.counters = w->counters.as<int>();
+  p.work_next = w->work_next.as<unsigned long long>();
+  p.film_acc = w->film_acc.as<double>();
+  p.film_out = ctx->film.as<float>();
+  if (use_graph && !w->exec && !w->graph_failed) {
+    if (build_graph(ctx, w) != BN_OK) {
+      w->graph_failed = true;  // fall back to the host-driven loop; the message stays in ctx->err
+      use_graph = false;
+    }
+  }
+  if (use_graph && !w->exec) use_graph = false;
+  p.cond = w->cond;
+  cudaStream_t st = ctx->stream;
+  cudaMemcpyAsync(w->params.ptr, &p, sizeof(p), cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(w->counters.ptr, 0, bn::kCntSize * sizeof(int), st);
+  cudaMemsetAsync(w->work_next.ptr, 0, sizeof(unsigned long long), st);
+  cudaMemsetAsync(w->meta.ptr, 0, static_cast<size_t>(pool) * sizeof(int4), st);
+  cudaMemsetAsync(w->film_acc.ptr, 0, static_cast<size_t>(n_pixels) * 3 * sizeof(double), st);
+  cudaEventRecord(ctx->ev0, st);
+  int launches = 0;
+  if (use_graph) {
+    if ((e = cudaGraphLaunch(w->exec, st)) != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphLaunch");
+  } else {
+    for (int it = 0; it < p.max_iters + 1; ++it) {
+      if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st)) != cudaSuccess)
+        return ctx->cuda_fail(e, "wavefront iteration launch");
+      launches += 5;
+      int again = 0;
+      cudaMemcpyAsync(&again, w->counters.as<int>() + bn::kCntAgain, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront iteration");
+      if (!again) break;
+    }
+  }
+  cudaEventRecord(ctx->ev1, st);
+  if ((e = bn::wf_launch_resolve(w->params.as<bn::WfParams>(), st)) != cudaSuccess)
+    return ctx->cuda_fail(e, "wavefront resolve");
+  cudaEventRecord(ctx->ev2, st);
+  if ((e = cudaEventSynchronize(ctx->ev2)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront render");
+  int counters[bn::kCntSize];
+  cudaMemcpy(counters, w->counters.ptr, sizeof(counters), cudaMemcpyDeviceToHost);
+  float ms_loop = 0.f, ms_all = 0.f;
+  cudaEventElapsedTime(&ms_loop, ctx->ev0, ctx->ev1);
+  cudaEventElapsedTime(&ms_all, ctx->ev0, ctx->ev2);
+  if (use_graph) launches = 5 * counters[bn::kCntIter];
+  ctx->stats.last_kernel_ms = ms_all;
+  ctx->stats.last_dominant_ms = ms_loop;
+  ctx->stats.last_launches = launches + 1;
+  if (ms_out) *ms_out = ms_all;
+  return BN_OK;
+}
+
+}  // namespace
+
+namespace bnc {
+
+int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views) {
+  WfState* w = state(ctx);
+  long long pixels = 0, total = 0;
+  for (const auto& v : views) {
+    pixels += static_cast<long long>(v.width) * v.height;
+    total += static_cast<long long>(v.width) * v.height * d->spp;
+  }
+  const bool use_graph = !(d->flags & BN_RENDER_NO_GRAPH);
+  int pool = d->queue_capacity, cap = d->block_size;  // block_size doubles as the blocks/SM cap
+  if (pool <= 0 && cap <= 0) {
+    const bool wt = d->flags & BN_RENDER_WATERTIGHT;
+    if (w->tuned_generation != ctx->scene_generation || w->tuned_watertight != wt) {
+      // autotune on a truncated render of the same views: pool size x blocks-per-SM cap
+      const int pools[3] = {1 << 19, 1 << 20, 1 << 21};
+      const int caps[2] = {0, 2};
+      const long long sample = std::min<long long>(total, 6LL << 20);
+      float best = 1e30f;
+      for (int pi : pools)
+        for (int ci : caps) {
+          float ms = 0.f;
+          const int rc = run(ctx, w, d, pixels, sample, static_cast<int>(views.size()), pi, ci, use_graph, &ms);
+          if (rc) return rc;
+          if (ms < best) {
+            best = ms;
+            w->tuned_pool = pi;
+            w->tuned_cap = ci;
+          }
+        }
+      w->tuned_generation = ctx->scene_generation;
+      w->tuned_watertight = wt;
+    }
+    pool = w->tuned_pool;
+    cap = w->tuned_cap;
+  }
+  if (pool <= 0) pool = 1 << 20;
+  pool = std::max(pool, 1024);
+  const int rc = run(ctx, w, d, pixels, total, static_cast<int>(views.size()), pool, cap, use_graph, nullptr);
+  if (rc) return rc;
+  ctx->stats.paths += static_cast<uint64_t>(total);
+  return BN_OK;
+}
+
+}  // namespace bnc

@@ -1,0 +1,365 @@
+// The batched wavefront form of PathTracingIntegrator.Li (PathTracing.fs:14-81) over many views.
+//
+// A pool of P path slots lives in HBM (SoA).  One iteration of the bounce loop is five kernels:
+//   regen    every slot: retire a finished path into the FP64 film, refill free slots with new
+//            camera paths (warp-aggregated claims on a global path counter), and append the
+//            active slots to the ray queue (ballot + popc compaction)
+//   extend   closest hit for the ray queue; each hit is binned by the material type it shades
+//            with (__match_any_sync groups, one atomic per group) so shading runs type-sorted
+//   shade    emission with MIS, light sample + BSDF eval (a shadow-ray record), BSDF sample,
+//            Russian roulette; marks paths that end
+//   shadow   any hit for the shadow queue; unoccluded records add their NEE term to L
+//   control  one thread: decides whether another iteration is needed, resets the counters and
+//            sets the CUDA-graph while-condition (or a flag for host-driven loops); an iteration
+//            cap stops a runaway loop with BN_DEVERR_WATCHDOG.
+// The arithmetic per path is the megakernel's (same helpers, same draw order, same operation
+// order), so both forms produce the same per-path radiance; only the film summation order
+// differs.  Kernels are persistent grid-stride loops whose trip counts come from device counters,
+// so one captured graph serves every iteration.
+#include "dev_shading.cuh"
+#include "wavefront.hpp"
+
+namespace bn {
+namespace {
+
+constexpr int kStatusFree = 0, kStatusActive = 1, kStatusDone = 2;
+constexpr int kBinMiss = 4, kBinNoMaterial = 5;
+
+__device__ __forceinline__ int warp_append(int* counter, bool pred) {
+  // ballot + popc compaction: one atomic per warp
+  const unsigned mask = __ballot_sync(0xffffffffu, pred);
+  int base = 0;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  if (lane == leader && mask) base = atomicAdd(counter, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader < 0 ? 0 : leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ int find_view(const WfParams& p, long long id) {
+  int v = 0;
+  while (v + 1 < p.n_views && p.views[v + 1].path_offset <= id) ++v;
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  const float inv_spp = __frcp_rn(static_cast<float>(p.spp));
+  const int stride = gridDim.x * blockDim.x;
+  // the loop runs in whole warps so the warp-wide claims and appends see all 32 lanes
+  const int n = (p.pool + 31) & ~31;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int slot = base + threadIdx.x;
+    const bool valid = slot < p.pool;
+    int4 m = valid ? p.meta[slot] : make_int4(0, 0, 0, kStatusActive);
+    if (valid && m.w == kStatusDone) {
+      const float4 L = p.L[slot];
+      double* f = p.film_acc + 3LL * m.x;
+      atomicAdd(f, static_cast<double>(__fmul_rn(L.x, inv_spp)));
+      atomicAdd(f + 1, static_cast<double>(__fmul_rn(L.y, inv_spp)));
+      atomicAdd(f + 2, static_cast<double>(__fmul_rn(L.z, inv_spp)));
+      m.w = kStatusFree;
+    }
+    // claim new paths for free slots
+    const bool want = valid && m.w == kStatusFree;
+    const unsigned wmask = __ballot_sync(0xffffffffu, want);
+    if (wmask) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(wmask) - 1;
+      unsigned long long first = 0;
+      if (lane == leader) first = atomicAdd(p.work_next, static_cast<unsigned long long>(__popc(wmask)));
+      first = __shfl_sync(0xffffffffu, first, leader);
+      const long long id = static_cast<long long>(first) + __popc(wmask & ((1u << lane) - 1u));
+      if (want && id < p.total_paths) {
+        const int vi = find_view(p, id);
+        const DevView& v = p.views[vi];
+        const long long local = id - v.path_offset;
+        const long long npix = static_cast<long long>(v.width) * v.height;
+        const int sid = static_cast<int>(local / npix);
+        const long long pix = local - sid * npix;
+        const int x = static_cast<int>(pix % v.width), y = static_cast<int>(pix / v.width);
+        IndepSampler smp{xxhash32_three(static_cast<uint32_t>(x), static_cast<uint32_t>(y),
+                                        static_cast<uint32_t>(p.frame_id * p.spp + sid))};
+        const float upx = smp.next(), upy = smp.next();
+        const float ulx = smp.next(), uly = smp.next();
+        const Ray ray = camera_ray(v, x, y, upx, upy, ulx, uly);
+        p.ray_o[slot] = make_float4(ray.o.x, ray.o.y, ray.o.z, 0.f);
+        p.ray_d[slot] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f);  // .w: pdf of the last BSDF sample
+        p.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+        p.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const long long film_pix = v.pixel_offset + static_cast<long long>(v.height - y - 1) * v.width + x;
+        m = make_int4(static_cast<int>(film_pix), 0, static_cast<int>(smp.state), kStatusActive);
+        if (p.max_depth <= 0) m.w = kStatusDone;  // while (depth < maxDepth) never runs
+      }
+    }
+    const bool active = valid && m.w == kStatusActive;
+    const int qi = warp_append(&p.counters[kCntActive], active);
+    if (active) p.q_active[qi] = slot;
+    if (valid) p.meta[slot] = m;
+  }
+}
+
+template <bool kWT>
+__global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  const DevScene& s = p.scene;
+  const int n = p.counters[kCntActive];
+  const int stride = gridDim.x * blockDim.x;
+  const int nw = (n + 31) & ~31;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
+    const bool valid = i < n;
+    int bin = kBinMiss;
+    int slot = 0;
+    if (valid) {
+      slot = p.q_active[i];
+      const float4 o = p.ray_o[slot], d = p.ray_d[slot];
+      Ray ray;
+      ray.o = mk(o.x, o.y, o.z);
+      ray.d = mk(d.x, d.y, d.z);
+      HitRec h;
+      TraceCounters tc;
+      if (trace_closest<kWT, false>(s, ray, CUDART_INF_F, &h, &tc)) {
+        p.hit_f[slot] = make_float4(h.t, h.u, h.v, 0.f);
+        p.hit_i[slot] = make_int2(h.inst, h.sphere_root ? h.sphere_root : h.tri);
+        const DevInstance* I = s.inst + h.inst;
+        int m = __ldg(&I->material);
+        if (m >= 0 && __ldg(&I->prim_type) == kPrimMesh) {
+          const int slot_m = __float_as_int(__ldg(&s.tris[3 * (__ldg(&I->tri_base) + h.tri)].w));
+          if (slot_m >= 0) m = slot_m;
+        }
+        bin = m < 0 ? kBinNoMaterial : s.mats[m].type;
+      } else {
+        p.hit_i[slot] = make_int2(-1, 0);
+      }
+    }
+    // material binning: lanes with equal keys share one atomic
+    const unsigned peers = __match_any_sync(0xffffffffu, valid ? bin : -1);
+    if (valid) {
+      const int leader = __ffs(peers) - 1;
+      const int lane = threadIdx.x & 31;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&p.counters[kCntBin0 + bin], __popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      const int pos = base + __popc(peers & ((1u << lane) - 1u));
+      p.q_bins[static_cast<long long>(bin) * p.pool + pos] = slot;
+    }
+  }
+}
+
+template <bool kWT>
+__global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  const DevScene& s = p.scene;
+  int cnt[kNumBins], total = 0;
+  for (int b = 0; b < kNumBins; ++b) { cnt[b] = p.counters[kCntBin0 + b]; total += cnt[b]; }
+  const int stride = gridDim.x * blockDim.x;
+  const int nw = (total + 31) & ~31;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
+    const bool valid = i < total;
+    bool done = false, cont = false, shadow = false;
+    int slot = 0;
+    float4 sh_o, sh_d, sh_a, sh_b;
+    if (valid) {
+      int b = 0, off = i;
+      while (off >= cnt[b]) { off -= cnt[b]; ++b; }
+      slot = p.q_bins[static_cast<long long>(b) * p.pool + off];
+      int4 m = p.meta[slot];
+      const int2 hi = p.hit_i[slot];
+      if (hi.x < 0) {
+        done = true;
+      } else {
+        const float4 o = p.ray_o[slot], d = p.ray_d[slot];
+        Ray ray;
+        ray.o = mk(o.x, o.y, o.z);
+        ray.d = mk(d.x, d.y, d.z);
+        const float pdf_bsdf = d.w;
+        const float4 hf = p.hit_f[slot];
+        HitRec h;
+        h.t = hf.x; h.u = hf.y; h.v = hf.z;
+        h.inst = hi.x;
+        const bool sphere = __ldg(&s.inst[hi.x].prim_type) == kPrimSphere;
+        h.tri = sphere ? 0 : hi.y;
+        h.sphere_root = sphere ? hi.y : 0;
+        const Interaction it = make_interaction(s, ray, h);
+        const float4 b4 = p.beta[slot];
+        V3 beta = mk(b4.x, b4.y, b4.z);
+        float4 L4 = p.L[slot];
+        V3 L = mk(L4.x, L4.y, L4.z);
+        const int depth = m.y;
+        const DevInstance* I = s.inst + it.inst;
+        if (__ldg(&I->light) >= 0) {
+          V3 le;
+          float pdf_l;
+          eval_light(s, ray.o, it, &le, &pdf_l);
+          const float mis = depth == 0 ? 1.f : __fmul_rn(pdf_bsdf, __frcp_rn(__fadd_rn(pdf_l, pdf_bsdf)));
+          L = fma3(beta, scale(mis, le), L);
+        }
+        const int mat = hit_material(s, it);
+        IndepSampler smp{static_cast<uint32_t>(m.z)};
+        if (mat < 0) {
+          done = true;
+        } else {
+          const float u_sel = smp.next(), ulx = smp.next(), uly = smp.next();
+          const DevMaterial mt = s.mats[mat];
+          const V3 wo_w = neg(ray.d);
+          const LightSample ls = sample_light(s, it.p, u_sel, ulx, uly);
+          const float dist = length(sub(ls.p, it.p));
+          if (ls.pdf != 0.f) {
+            const BsdfEval be = bsdf_eval(mt, to_local(it.f, wo_w), to_local(it.f, ls.wi));
+            const V3 a = mul(beta, be.f);
+            const V3 bb = scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L);
+            sh_o = make_float4(it.p.x, it.p.y, it.p.z, __fsub_rn(dist, 1e-3f));
+            sh_d = make_float4(ls.wi.x, ls.wi.y, ls.wi.z, __int_as_float(slot));
+            sh_a = make_float4(a.x, a.y, a.z, 0.f);
+            sh_b = make_float4(bb.x, bb.y, bb.z, 0.f);
+            shadow = true;
+          }
+          const float u_lobe = smp.next(), ubx = smp.next(), uby = smp.next();
+          const BsdfSample bs = bsdf_sample(mt, to_local(it.f, wo_w), u_lobe, ubx, uby);
+          if (bs.pdf == 0.f) {
+            done = true;
+          } else {
+            const V3 nd = to_world(it.f, bs.wi);
+            beta = scale(__frcp_rn(bs.pdf), mul(beta, bs.f));
+            bool alive = true;
+            if (depth >= p.rr_depth) {
+              const float q = fminf(1.f, fmaxf(beta.x, fmaxf(beta.y, beta.z)));
+              if (smp.next() < q) beta = scale(__frcp_rn(q), beta);
+              else alive = false;
+            }
+            if (alive && depth + 1 < p.max_depth) {
+              cont = true;
+              p.ray_o[slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
+              p.ray_d[slot] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
+              p.beta[slot] = make_float4(beta.x, beta.y, beta.z, 0.f);
+              m.y = depth + 1;
+            } else {
+              done = true;
+            }
+          }
+        }
+        p.L[slot] = make_float4(L.x, L.y, L.z, 0.f);
+        m.z = static_cast<int>(smp.state);
+      }
+      if (done) m.w = kStatusDone;
+      p.meta[slot] = m;
+    }
+    const int si = warp_append(&p.counters[kCntShadow], shadow);
+    if (shadow) {
+      float4* r = p.shadow + 4LL * si;
+      r[0] = sh_o; r[1] = sh_d; r[2] = sh_a; r[3] = sh_b;
+    }
+    const unsigned cm = __ballot_sync(0xffffffffu, cont), dm = __ballot_sync(0xffffffffu, done);
+    if ((threadIdx.x & 31) == 0) {
+      if (cm) atomicAdd(&p.counters[kCntCont], __popc(cm));
+      if (dm) atomicAdd(&p.counters[kCntDone], __popc(dm));
+    }
+  }
+}
+
+template <bool kWT>
+__global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  const int n = p.counters[kCntShadow];
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float4* r = p.shadow + 4LL * i;
+    const float4 o = r[0], d = r[1];
+    Ray ray;
+    ray.o = mk(o.x, o.y, o.z);
+    ray.d = mk(d.x, d.y, d.z);
+    TraceCounters tc;
+    if (!trace_any<kWT, false>(p.scene, ray, o.w, &tc)) {
+      const int slot = __float_as_int(d.w);
+      const float4 a = r[2], b = r[3];
+      float4 L = p.L[slot];
+      L.x = fmaf(a.x, b.x, L.x);
+      L.y = fmaf(a.y, b.y, L.y);
+      L.z = fmaf(a.z, b.z, L.z);
+      p.L[slot] = L;
+    }
+  }
+}
+
+__global__ void k_wf_control(WfParams* pp, int use_graph) {
+  WfParams& p = *pp;
+  int* c = p.counters;
+  const bool more_work = *p.work_next < static_cast<unsigned long long>(p.total_paths);
+  bool again = c[kCntCont] > 0 || c[kCntDone] > 0 || more_work;
+  const int iter = ++c[kCntIter];
+  if (again && iter >= p.max_iters) {
+    atomicOr(p.scene.error_word, BN_DEVERR_WATCHDOG);
+    again = false;
+  }
+  c[kCntActive] = 0;
+  c[kCntShadow] = 0;
+  c[kCntCont] = 0;
+  c[kCntDone] = 0;
+  for (int b = 0; b < kNumBins; ++b) c[kCntBin0 + b] = 0;
+  c[kCntAgain] = again ? 1 : 0;
+  if (use_graph) cudaGraphSetConditional(p.cond, again ? 1u : 0u);
+}
+
+// FP64 film -> FP32 film (the rows were flipped when the pixel index was formed)
+__global__ void k_wf_resolve(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  const long long n = 3LL * p.n_pixels;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    p.film_out[i] = static_cast<float>(p.film_acc[i]);
+}
+
+template <class K>
+int resident_grid(K kernel, int block) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0);
+  return sms * (per > 0 ? per : 1);
+}
+
+}  // namespace
+
+cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st) {
+  k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
+  if (l.watertight) {
+    k_wf_extend<true><<<l.grid_extend, 128, 0, st>>>(dparams);
+    k_wf_shade<true><<<l.grid_shade, 128, 0, st>>>(dparams);
+    k_wf_shadow<true><<<l.grid_shadow, 128, 0, st>>>(dparams);
+  } else {
+    k_wf_extend<false><<<l.grid_extend, 128, 0, st>>>(dparams);
+    k_wf_shade<false><<<l.grid_shade, 128, 0, st>>>(dparams);
+    k_wf_shadow<false><<<l.grid_shadow, 128, 0, st>>>(dparams);
+  }
+  k_wf_control<<<1, 1, 0, st>>>(dparams, use_graph ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
+  k_wf_resolve<<<152 * 8, 256, 0, st>>>(dparams);
+  return cudaGetLastError();
+}
+
+WfLaunch wf_launch_shape(bool watertight, int blocks_per_sm_cap) {
+  WfLaunch l{};
+  l.watertight = watertight;
+  auto cap = [&](int g) {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return blocks_per_sm_cap > 0 ? std::min(g, sms * blocks_per_sm_cap) : g;
+  };
+  l.grid_regen = cap(resident_grid(k_wf_regen, 256));
+  if (watertight) {
+    l.grid_extend = cap(resident_grid(k_wf_extend<true>, 128));
+    l.grid_shade = cap(resident_grid(k_wf_shade<true>, 128));
+    l.grid_shadow = cap(resident_grid(k_wf_shadow<true>, 128));
+  } else {
+    l.grid_extend = cap(resident_grid(k_wf_extend<false>, 128));
+    l.grid_shade = cap(resident_grid(k_wf_shade<false>, 128));
+    l.grid_shadow = cap(resident_grid(k_wf_shadow<false>, 128));
+  }
+  return l;
+}
+
+}  // namespace bn

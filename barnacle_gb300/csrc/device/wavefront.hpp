@@ -1,0 +1,59 @@
+// Wavefront path state (HBM, structure of arrays) and launch interface.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../../include/barnacle_gpu.h"
+#include "dev_types.cuh"
+
+namespace bn {
+
+constexpr int kNumBins = 6;  // 4 material types, miss, no material
+enum : int {
+  kCntActive = 0,   // ray-queue length
+  kCntShadow = 1,   // shadow-queue length
+  kCntCont = 2,     // paths continuing after shade
+  kCntDone = 3,     // paths that ended this iteration (retired by the next regen)
+  kCntIter = 4,     // iterations run
+  kCntAgain = 5,    // last control decision (host-driven loop)
+  kCntBin0 = 8,     // 8..13: per-bin hit counts
+  kCntSize = 16
+};
+
+struct WfParams {
+  DevScene scene;
+  const DevView* views;
+  int n_views;
+  int spp, max_depth, rr_depth, frame_id;
+  int pool;                     // path slots
+  int max_iters;                // watchdog
+  long long total_paths;
+  long long n_pixels;
+  // per slot
+  float4* ray_o;                // (o, -)
+  float4* ray_d;                // (d, pdf of the last BSDF sample)
+  float4* beta;
+  float4* L;
+  int4* meta;                   // (film pixel, depth, sampler state, status)
+  float4* hit_f;                // (t, u, v, -)
+  int2* hit_i;                  // (instance | -1, triangle or sphere root)
+  // queues
+  int* q_active;                // pool entries
+  int* q_bins;                  // kNumBins x pool entries
+  float4* shadow;               // 4 float4 per record: (o, tmax), (d, owner), a, b
+  int* counters;                // kCntSize ints
+  unsigned long long* work_next;
+  double* film_acc;             // 3 doubles per pixel
+  float* film_out;              // 3 floats per pixel
+  cudaGraphConditionalHandle cond;
+};
+
+struct WfLaunch {
+  int grid_regen, grid_extend, grid_shade, grid_shadow;
+  bool watertight;
+};
+
+WfLaunch wf_launch_shape(bool watertight, int blocks_per_sm_cap);
+cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
+cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st);
+
+}  // namespace bn

@@ -22,6 +22,7 @@ Multi-GPU (torchrun): every rank renders the full workload (replicas, weak scali
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -190,7 +191,8 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--mode", default="wavefront", choices=["megakernel", "wavefront"])
+    ap.add_argument("--no-compare", action="store_true", help="skip timing the other render form")
     ap.add_argument("--spp-per-step", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -209,7 +211,6 @@ def main():
     views = b.views
     r = b.render
     r.spp = args.spp_per_step
-    r.mode = capi.BN_MODE_WAVEFRONT if args.mode == "wavefront" else capi.BN_MODE_MEGAKERNEL
     pixels = sum(v.width * v.height for v in views)
     paths_per_step = pixels * r.spp
     torch.cuda.set_device(dev)
@@ -218,10 +219,10 @@ def main():
     # algorithmic bytes per launch of the dominant kernel: an instrumented run of one step
     rc = capi.bn_render_desc()
     C_copy = bytes(r)
-    import ctypes as C
     C.memmove(C.addressof(rc), C_copy, len(C_copy))
     rc.flags |= capi.BN_RENDER_COUNT
-    rc.frame_id = 10_000
+    rc.mode = capi.BN_MODE_MEGAKERNEL  # both forms trace the same rays; the megakernel counts them
+    rc.frame_id = 100
     ctx.reset_stats()
     ctx.render(rc, views, to_host=False)
     st = ctx.stats()
@@ -229,18 +230,19 @@ def main():
     alg_bytes = bpu["node"] * st.nodes_visited + bpu["triangle"] * st.tris_tested + bpu["instance"] * st.instances_visited
     rays_per_step = st.rays
 
-    for w in range(args.warmup):
-        r.frame_id = w
-        ctx.render(r, views, to_host=False)
-    barrier(dist)
-    torch.cuda.synchronize()
-    dev_ms, dom_ms, launches = 0.0, 0.0, 0
-    with ClockSampler(dev) as clk:
+    def timed(mode, frame_base):
+        r.mode = mode
+        for w in range(args.warmup):
+            r.frame_id = frame_base + w
+            ctx.render(r, views, to_host=False)
+        barrier(dist)
+        torch.cuda.synchronize()
+        dev_ms, dom_ms, launches = 0.0, 0.0, 0
         t0 = time.perf_counter()
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            r.frame_id = 100 + k
+            r.frame_id = frame_base + 100 + k
             ctx.render(r, views, to_host=False)
             s = ctx.stats()
             dev_ms += s.last_kernel_ms
@@ -248,10 +250,19 @@ def main():
             launches += s.last_launches
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    barrier(dist)
-    dev_s = max_over_ranks(dist, dev_ms / 1000.0)
+        barrier(dist)
+        return max_over_ranks(dist, dev_ms / 1000.0), dom_ms, launches, wall
+
+    primary = capi.BN_MODE_WAVEFRONT if args.mode == "wavefront" else capi.BN_MODE_MEGAKERNEL
+    other = capi.BN_MODE_MEGAKERNEL if primary == capi.BN_MODE_WAVEFRONT else capi.BN_MODE_WAVEFRONT
+    with ClockSampler(dev) as clk:
+        dev_s, dom_ms, launches, wall = timed(primary, 0)
+    other_s = None
+    if not args.no_compare:
+        other_s, _, _, _ = timed(other, 1000)
 
     # end to end through the C-ABI with a host film (pinned)
+    r.mode = primary
     film = torch.empty(pixels * 3, dtype=torch.float32).pin_memory().numpy()
     view_arr = (capi.bn_view * len(views))(*views)
     barrier(dist)
@@ -289,11 +300,15 @@ def main():
             "config": {"workload": f"{WORKLOAD}: 1024 instances of 4 displaced icospheres (20k/82k/200k/328k tris) "
                                    "+ 64 emissive triangles, 16 views 256x240..1920x1080, depth 12, rr 3",
                        "mode": args.mode, "spp_per_step": r.spp, "pixels_per_step": pixels,
-                       "rays_per_step": int(rays_per_step), "parallelism": "replicas" if world > 1 else "single",
+                       "rays_per_step": int(rays_per_step),
+                       "per_ray": {"nodes": st.nodes_visited / max(1, st.rays), "triangles": st.tris_tested / max(1, st.rays),
+                                   "instances": st.instances_visited / max(1, st.rays)},
+                       "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed before every timed step (512 MiB write)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_pt_mega" if args.mode == "megakernel" else "wavefront extend",
+                         "kernel": "k_pt_mega" if args.mode == "megakernel" else
+                                   "wavefront bounce loop (regen+extend+shade+shadow, one graph)",
                          "alg_bytes_per_launch": int(alg_bytes)},
             "cpu_baseline": cpu,
             "e2e": {"value": world * paths_per_step * args.steps / e2e_s, "unit": "paths/s",
@@ -302,6 +317,12 @@ def main():
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "mrays_per_s": world * rays_per_step * args.steps / dev_s / 1e6,
+            "compare": None if other_s is None else {
+                "other_mode": "megakernel" if primary == capi.BN_MODE_WAVEFRONT else "wavefront",
+                "other_paths_per_s": world * paths_per_step * args.steps / other_s,
+                "ratio_this_over_other": other_s / dev_s,
+                "equal_rmse": "same per-path estimator and random streams in both forms (images equal to "
+                              "float summation order, tests/test_gpu_wavefront.py)"},
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)
