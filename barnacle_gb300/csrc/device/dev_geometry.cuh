@@ -237,161 +237,15 @@ struct HitRec {
   int sphere_root;  // 1 near root, 2 far root (spheres only)
 };
 
-constexpr int kStackSize = 136;  // TLAS (<= 65) + BLAS (<= 65) entries of a depth-64 BVH pair
-
 __device__ __forceinline__ void flag_error(const DevScene& s, unsigned bit) {
   if (s.error_word) atomicOr(s.error_word, bit);
 }
 
-// PrimitiveAggregate.Intersect(ray, &interaction, &t): TLAS closest hit (Aggregate/BVH.fs:37-58)
-// -> PrimitiveInstance.Intersect (Primitive.fs:118-129) -> MeshPrimitive.Intersect
-// (Mesh.fs:217-242) or SpherePrimitive.Intersect.  Near child first when d[axis] > 0.
-template <bool kWatertight, bool kCount>
-__device__ __forceinline__ bool trace_closest(const DevScene& s, const Ray& ray, float tmax, HitRec* hit, TraceCounters* cnt) {
-  int stack[kStackSize];
-  int sp = 0;
-  stack[sp++] = 0;
-  const V3 inv = inv_dir(ray.d);
-  float t = tmax;
-  bool found = false;
-  hit->inst = -1;
-  while (sp > 0) {
-    const int ni = stack[--sp];
-    const NodeRec n = load_node(s.nodes, ni);
-    if (kCount) cnt->nodes++;
-    if (!box_hit(n.bmin, n.bmax, ray, inv, t)) continue;
-    if (!n.leaf) {
-      if (sp + 2 > kStackSize) { flag_error(s, BN_DEVERR_STACK_OVERFLOW); break; }
-      if (comp(ray.d, n.axis) > 0.f) { stack[sp++] = n.link; stack[sp++] = ni + 1; }
-      else { stack[sp++] = ni + 1; stack[sp++] = n.link; }
-      continue;
-    }
-    for (int k = n.link; k < n.link + n.count; ++k) {
-      const DevInstance* I = s.inst + k;
-      if (kCount) cnt->insts++;
-      const float4 bmin = __ldg(&I->bmin), bmax = __ldg(&I->bmax);
-      if (!box_hit(xyz(bmin), xyz(bmax), ray, inv, t)) continue;
-      float4 w2o[3];
-      load_xf(I->w2o, w2o);
-      Ray oray;
-      oray.o = xf_point(w2o, ray.o);
-      oray.d = xf_dir(w2o, ray.d);
-      const int ptype = __ldg(&I->prim_type);
-      if (ptype == kPrimSphere) {
-        float ts;
-        const int root = sphere_hit(bmax.w, oray, t, &ts);
-        if (root) {
-          t = ts; found = true;
-          hit->inst = k; hit->tri = 0; hit->sphere_root = root; hit->t = ts; hit->u = 0.f; hit->v = 0.f;
-        }
-        continue;
-      }
-      const int node_base = __ldg(&I->node_base), tri_base = __ldg(&I->tri_base);
-      const V3 oinv = inv_dir(oray.d);
-      WtRay wt;
-      if (kWatertight) wt = wt_setup(oray.d);
-      int bsp = sp;
-      stack[bsp++] = 0;
-      while (bsp > sp) {
-        const int bi = stack[--bsp];
-        const NodeRec bn = load_node(s.nodes, node_base + bi);
-        if (kCount) cnt->nodes++;
-        if (!box_hit(bn.bmin, bn.bmax, oray, oinv, t)) continue;
-        if (!bn.leaf) {
-          if (bsp + 2 > kStackSize) { flag_error(s, BN_DEVERR_STACK_OVERFLOW); bsp = sp; break; }
-          if (comp(oray.d, bn.axis) > 0.f) { stack[bsp++] = bn.link; stack[bsp++] = bi + 1; }
-          else { stack[bsp++] = bi + 1; stack[bsp++] = bn.link; }
-          continue;
-        }
-        for (int j = bn.link; j < bn.link + bn.count; ++j) {
-          const float4* tp = s.tris + 3 * (tri_base + j);
-          const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-          if (kCount) cnt->tris++;
-          const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
-          float tt, uu, vv;
-          // the triangle's own AABB pre-test (Mesh.fs:231; its 1e-3 near bound is part of the
-          // reference's self-intersection behaviour), then the triangle test
-          const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
-          bool h = box_hit(lo, hi, oray, oinv, t);
-          if (h) h = kWatertight ? tri_wt(p0, p1, p2, oray, wt, t, &tt, &uu, &vv) : tri_mt(p0, p1, p2, oray, t, &tt, &uu, &vv);
-          if (h) {
-            t = tt; found = true;
-            hit->inst = k; hit->tri = j; hit->t = tt; hit->u = uu; hit->v = vv; hit->sphere_root = 0;
-          }
-        }
-      }
-    }
-  }
-  return found;
-}
+}  // namespace bn
 
-// PrimitiveAggregate.Intersect(ray, t): TLAS any hit (Aggregate/BVH.fs:11-35) ->
-// MeshPrimitive.Intersect(ray, t) (Mesh.fs:188-215).  Stops at the first hit.
-template <bool kWatertight, bool kCount>
-__device__ __forceinline__ bool trace_any(const DevScene& s, const Ray& ray, float tmax, TraceCounters* cnt) {
-  int stack[kStackSize];
-  int sp = 0;
-  stack[sp++] = 0;
-  const V3 inv = inv_dir(ray.d);
-  while (sp > 0) {
-    const int ni = stack[--sp];
-    const NodeRec n = load_node(s.nodes, ni);
-    if (kCount) cnt->nodes++;
-    if (!box_hit(n.bmin, n.bmax, ray, inv, tmax)) continue;
-    if (!n.leaf) {
-      if (sp + 2 > kStackSize) { flag_error(s, BN_DEVERR_STACK_OVERFLOW); return false; }
-      if (comp(ray.d, n.axis) > 0.f) { stack[sp++] = n.link; stack[sp++] = ni + 1; }
-      else { stack[sp++] = ni + 1; stack[sp++] = n.link; }
-      continue;
-    }
-    for (int k = n.link; k < n.link + n.count; ++k) {
-      const DevInstance* I = s.inst + k;
-      if (kCount) cnt->insts++;
-      const float4 bmin = __ldg(&I->bmin), bmax = __ldg(&I->bmax);
-      if (!box_hit(xyz(bmin), xyz(bmax), ray, inv, tmax)) continue;
-      float4 w2o[3];
-      load_xf(I->w2o, w2o);
-      Ray oray;
-      oray.o = xf_point(w2o, ray.o);
-      oray.d = xf_dir(w2o, ray.d);
-      if (__ldg(&I->prim_type) == kPrimSphere) {
-        float ts;
-        if (sphere_hit(bmax.w, oray, tmax, &ts)) return true;
-        continue;
-      }
-      const int node_base = __ldg(&I->node_base), tri_base = __ldg(&I->tri_base);
-      const V3 oinv = inv_dir(oray.d);
-      WtRay wt;
-      if (kWatertight) wt = wt_setup(oray.d);
-      int bsp = sp;
-      stack[bsp++] = 0;
-      while (bsp > sp) {
-        const int bi = stack[--bsp];
-        const NodeRec bn = load_node(s.nodes, node_base + bi);
-        if (kCount) cnt->nodes++;
-        if (!box_hit(bn.bmin, bn.bmax, oray, oinv, tmax)) continue;
-        if (!bn.leaf) {
-          if (bsp + 2 > kStackSize) { flag_error(s, BN_DEVERR_STACK_OVERFLOW); return false; }
-          if (comp(oray.d, bn.axis) > 0.f) { stack[bsp++] = bn.link; stack[bsp++] = bi + 1; }
-          else { stack[bsp++] = bi + 1; stack[bsp++] = bn.link; }
-          continue;
-        }
-        for (int j = bn.link; j < bn.link + bn.count; ++j) {
-          const float4* tp = s.tris + 3 * (tri_base + j);
-          const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-          if (kCount) cnt->tris++;
-          const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
-          float tt, uu, vv;
-          const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
-          bool h = box_hit(lo, hi, oray, oinv, tmax);
-          if (h) h = kWatertight ? tri_wt(p0, p1, p2, oray, wt, tmax, &tt, &uu, &vv) : tri_mt(p0, p1, p2, oray, tmax, &tt, &uu, &vv);
-          if (h) return true;
-        }
-      }
-    }
-  }
-  return false;
-}
+#include "dev_traverse.cuh"
+
+namespace bn {
 
 // ------------------------------------------------------------------ surface interaction
 // The shading frame of a hit: LocalGeometry in object space, then LocalGeometry.Transform with

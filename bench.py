@@ -195,6 +195,9 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other render form")
     ap.add_argument("--spp-per-step", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="wavefront bounce loop driven from the host (ncu cannot profile kernels inside a "
+                         "graph with a conditional node)")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
@@ -211,6 +214,8 @@ def main():
     views = b.views
     r = b.render
     r.spp = args.spp_per_step
+    if args.no_graph:
+        r.flags |= capi.BN_RENDER_NO_GRAPH
     pixels = sum(v.width * v.height for v in views)
     paths_per_step = pixels * r.spp
     torch.cuda.set_device(dev)

@@ -35,6 +35,8 @@ def lib() -> C.CDLL:
             "or_bsdf": (C.c_int, [P, P, C.c_int64, C.c_int, C.c_int, P]),
             "or_render_pt": (C.c_int, [P, C.POINTER(capi.bn_render_desc), C.POINTER(capi.bn_view), C.c_int32,
                                        C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]),
+            "or_render_pssmlt": (C.c_int, [P, C.POINTER(capi.bn_render_desc), C.POINTER(capi.bn_view), C.c_int32,
+                                           P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -113,3 +115,12 @@ class Scene:
         threads = threads or os.cpu_count() or 1
         lib().or_render_pt(self._h, C.byref(desc), C.byref(view), x0, y0, x1, y1, threads, ptr(out), ptr(counts))
         return out, counts
+
+    def render_pssmlt(self, desc, view, threads: int | None = None):
+        """PSSMLTIntegrator.Render: returns (film (H, W, 3), b, accepted, proposed, bootstrap y)."""
+        out = np.zeros((view.height, view.width, 3), np.float32)
+        stats = np.zeros(3, np.float64)
+        boot = np.zeros(max(desc.n_bootstrap, 1), np.float32)
+        threads = threads or os.cpu_count() or 1
+        lib().or_render_pssmlt(self._h, C.byref(desc), C.byref(view), threads, ptr(out), ptr(stats), ptr(boot))
+        return out, float(stats[0]), int(stats[1]), int(stats[2]), boot

@@ -1028,6 +1028,115 @@ Vector3 Li(const Scene& sc, Ray ray, Smp& smp, int maxDepth, int rrDepth, bool w
   return L;
 }
 
+// ---------------------------------------------------------------- PSSMLT (PSSMLT.fs)
+// Giles' single-precision erfinv as the reference evaluates it (PSSMLT.fs:69-94)
+float ErfInv(float x) {
+  x = std::min(std::max(x, -0.99999f), 0.99999f);
+  float w = -std::log(std::fma(x, -x, 1.f));
+  float p;
+  if (w < 5.f) {
+    w = w - 2.5f;
+    p = 2.81022636e-08f;
+    p = std::fma(p, w, 3.43273939e-07f);
+    p = std::fma(p, w, -3.5233877e-06f);
+    p = std::fma(p, w, -4.39150654e-06f);
+    p = std::fma(p, w, 0.00021858087f);
+    p = std::fma(p, w, -0.00125372503f);
+    p = std::fma(p, w, -0.00417768164f);
+    p = std::fma(p, w, 0.246640727f);
+    return std::fma(p, w, 1.50140941f) * x;
+  }
+  w = std::sqrt(w) - 3.f;
+  p = -0.000200214257f;
+  p = std::fma(p, w, 0.000100950558f);
+  p = std::fma(p, w, 0.00134934322f);
+  p = std::fma(p, w, -0.00367342844f);
+  p = std::fma(p, w, 0.00573950773f);
+  p = std::fma(p, w, -0.0076224613f);
+  p = std::fma(p, w, 0.00943887047f);
+  p = std::fma(p, w, 1.00167406f);
+  return std::fma(p, w, 2.83297682f) * x;
+}
+
+struct PrimarySample {
+  float Value = 0, ValueBackUp = 0;
+  int LastModification = 0, ModificationBackUp = 0;
+};
+
+// MLTSampler (PSSMLT.fs:36-150)
+struct MLTSampler {
+  Sampler Inner;
+  float LargeStepProb;
+  bool kelemen;
+  float sigma, epsMin, epsMax;
+  PrimarySample* Xs;
+  bool LargeStep = false;
+  int LastLargeStepIteration = 0, CurrentIteration = 0, SampleIndex = 0, InitializedSampleCount = 0;
+
+  void StartIteration() {
+    LargeStep = CurrentIteration == 0 || Inner.Next1D() < LargeStepProb;
+    CurrentIteration = CurrentIteration + 1;
+    SampleIndex = 0;
+  }
+  float EnsureReady(int index) {
+    PrimarySample& x = Xs[index];
+    if (InitializedSampleCount <= index) {
+      x = PrimarySample{};
+      InitializedSampleCount = index + 1;
+    }
+    if (x.LastModification < LastLargeStepIteration) {
+      x.Value = Inner.Next1D();
+      x.LastModification = LastLargeStepIteration;
+    }
+    x.ValueBackUp = x.Value;
+    x.ModificationBackUp = x.LastModification;
+    float v;
+    if (LargeStep) {
+      v = Inner.Next1D();
+    } else if (!kelemen) {
+      const float normal = std::sqrt(2.f) * ErfInv(std::fma(2.f, Inner.Next1D(), -1.f));
+      const float eff = sigma * std::sqrt(static_cast<float>(CurrentIteration - x.LastModification));
+      v = std::fma(normal, eff, x.Value);
+    } else {
+      v = x.Value;
+      const float a = std::log(epsMax / epsMin);
+      for (int k = x.LastModification; k <= CurrentIteration - 1; ++k) {
+        const float u1 = Inner.Next1D() - 0.5f;
+        const float u2 = u1 < 0.f ? 1.f + 2.f * u1 : 2.f * u1;
+        v = v + std::copysign(epsMax * std::exp(-a * u2), u1);
+      }
+    }
+    x.Value = v - std::floor(v);
+    x.LastModification = CurrentIteration;
+    return x.Value;
+  }
+  float next() { return EnsureReady(SampleIndex++); }
+  void Reject() {
+    for (int i = 0; i < InitializedSampleCount; ++i) {
+      Xs[i].Value = Xs[i].ValueBackUp;
+      Xs[i].LastModification = Xs[i].ModificationBackUp;
+    }
+    CurrentIteration = CurrentIteration - 1;
+  }
+  void Accept() {
+    if (LargeStep) LastLargeStepIteration = CurrentIteration;
+  }
+};
+
+float Luminance(const Vector3& L) { return Vector3::Dot(L, Vector3(0.2126f, 0.7152f, 0.0722f)); }
+
+template <class Smp>
+Ray MltCamera(const Camera& cam, Smp& smp, int* px, int* py) {
+  const float ux = smp.next() * static_cast<float>(cam.W);
+  const float uy = smp.next() * static_cast<float>(cam.H);
+  const int x = std::min(cam.W - 1, static_cast<int>(ux)), y = std::min(cam.H - 1, static_cast<int>(uy));
+  const float fx = ux - static_cast<float>(x), fy = uy - static_cast<float>(y);
+  const float lx = smp.next(), ly = smp.next();
+  *px = x;
+  *py = y;
+  return cam.Generate(x, y, fx, fy, lx, ly);
+}
+
 std::unique_ptr<Scene> BuildScene(const bn_scene_desc* d) {
   auto sc = std::make_unique<Scene>();
   sc->meshes.resize(d->n_meshes);
@@ -1251,6 +1360,124 @@ int or_render_pt(const or_scene* os, const bn_render_desc* d, const bn_view* vie
     for (const auto& c : per) { tot.rays += c.rays; tot.nodes += c.nodes; tot.tris += c.tris; tot.insts += c.insts; }
     counts[0] = tot.rays; counts[1] = tot.nodes; counts[2] = tot.tris; counts[3] = tot.insts;
   }
+  return 0;
+}
+
+// PSSMLTIntegrator.Render (PSSMLT.fs:379-414).  Chains run on `threads` workers with their own
+// film copies, summed at the end (the reference's shared non-atomic film is racy).
+// out: W*H*3 floats; stats: [b, accepted, proposed].  bootstrap_out (optional): n_bootstrap y.
+int or_render_pssmlt(const or_scene* os, const bn_render_desc* d, const bn_view* view, int32_t threads, float* out,
+                     double* stats, float* bootstrap_out) {
+  const Scene& sc = *os->s;
+  const Camera cam = Camera::From(*view);
+  const int W = view->width, H = view->height;
+  const bool wt = d->flags & BN_RENDER_WATERTIGHT;
+  const int dims = 4 + 7 * d->max_depth;
+  const int nb = d->n_bootstrap, nc = d->n_chains;
+  const int T = std::max(threads, 1);
+  std::vector<float> weights(nb);
+  {
+    std::atomic<int> next{0};
+    auto boot = [&]() {
+      Counters c;
+      std::vector<PrimarySample> xs(dims);
+      for (;;) {
+        const int id = next.fetch_add(1);
+        if (id >= nb) break;
+        MLTSampler m{Sampler::Two(static_cast<uint32_t>(d->frame_id), static_cast<uint32_t>(id)), d->large_step_prob,
+                     d->mutation == BN_MUTATION_KELEMEN, d->sigma, d->eps_min, d->eps_max, xs.data()};
+        m.StartIteration();
+        int px, py;
+        const Ray ray = MltCamera(cam, m, &px, &py);
+        const Vector3 L = Li<true>(sc, ray, m, d->max_depth, d->rr_depth, wt, &c) * (1.f / 1.f);
+        weights[id] = Luminance(L);
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 0; w < T; ++w) pool.emplace_back(boot);
+    for (auto& t : pool) t.join();
+  }
+  if (bootstrap_out) std::memcpy(bootstrap_out, weights.data(), weights.size() * sizeof(float));
+  float sum = 0.f;
+  for (float x : weights) sum = sum + x;
+  const float B = sum / static_cast<float>(nb);
+  stats[0] = B;
+  const long long mpc = (static_cast<long long>(d->spp) * W * H + nc - 1) / nc;
+  stats[2] = static_cast<double>(mpc) * nc;
+  std::fill(out, out + 3LL * W * H, 0.f);
+  if (B == 0.f) { stats[1] = 0; return 0; }
+  // the AliasTable as built samples uniformly; with BN_RENDER_FIXED_ALIAS, proportionally to y
+  std::vector<TriLightEntry> table;
+  if (d->flags & BN_RENDER_FIXED_ALIAS) {
+    std::vector<double> w(nb);
+    for (int i = 0; i < nb; ++i) w[i] = weights[i] > 0.f ? weights[i] : 0.f;
+    table.resize(nb);
+    BuildVose(w, &table);
+  }
+  const float invEff = 1.f / ((static_cast<float>(mpc) * static_cast<float>(nc)) / static_cast<float>(W * H));
+  const float invB = 1.f / B;
+  std::atomic<int> next{0};
+  std::atomic<long long> accepted{0};
+  std::vector<std::vector<float>> films(T, std::vector<float>(3LL * W * H, 0.f));
+  auto chains = [&](int wi) {
+    Counters c;
+    std::vector<PrimarySample> xs(dims);
+    std::vector<float>& film = films[wi];
+    auto splat = [&](int x, int y, const Vector3& v) {
+      const size_t i = static_cast<size_t>(H - y - 1) * W + x;
+      film[3 * i] += v.X; film[3 * i + 1] += v.Y; film[3 * i + 2] += v.Z;
+    };
+    long long acc_local = 0;
+    for (;;) {
+      const int chain = next.fetch_add(1);
+      if (chain >= nc) break;
+      Sampler cs = Sampler::Two(static_cast<uint32_t>(d->frame_id), static_cast<uint32_t>(chain));
+      float u = cs.Next1D() * static_cast<float>(nb);
+      int bid = std::min(static_cast<int>(u), nb - 1);
+      if (!table.empty() && u - static_cast<float>(bid) >= table[bid].prob) bid = table[bid].alias;
+      MLTSampler m{Sampler::Two(static_cast<uint32_t>(d->frame_id), static_cast<uint32_t>(bid)), d->large_step_prob,
+                   d->mutation == BN_MUTATION_KELEMEN, d->sigma, d->eps_min, d->eps_max, xs.data()};
+      m.StartIteration();
+      int px, py;
+      Ray ray = MltCamera(cam, m, &px, &py);
+      Vector3 L = Li<true>(sc, ray, m, d->max_depth, d->rr_depth, wt, &c) * (1.f / 1.f);
+      float y = Luminance(L);
+      m.Accept();
+      m.Inner = Sampler::Three(static_cast<uint32_t>(chain), static_cast<uint32_t>(bid), static_cast<uint32_t>(d->frame_id));
+      Vector3 radiance(0.f);
+      for (long long it = 0; it < mpc; ++it) {
+        m.StartIteration();
+        int nx, ny;
+        ray = MltCamera(cam, m, &nx, &ny);
+        const Vector3 Ln = Li<true>(sc, ray, m, d->max_depth, d->rr_depth, wt, &c) * (1.f / 1.f);
+        const float yn = Luminance(Ln);
+        const float accept = MathMin(1.f, yn / y);
+        const float wOld = (1.f - accept) / std::fma(y, invB, d->large_step_prob);
+        radiance = radiance + wOld * L;
+        const float wNew = (accept + (m.LargeStep ? 1.f : 0.f)) / std::fma(yn, invB, d->large_step_prob);
+        if (cs.Next1D() < accept) {
+          ++acc_local;
+          splat(px, py, radiance * invEff);
+          radiance = wNew * Ln;
+          px = nx; py = ny;
+          L = Ln;
+          y = yn;
+          m.Accept();
+        } else {
+          if (accept > 0.f) splat(nx, ny, (wNew * invEff) * Ln);
+          m.Reject();
+        }
+      }
+      splat(px, py, radiance * invEff);
+    }
+    accepted += acc_local;
+  };
+  std::vector<std::thread> pool;
+  for (int w = 0; w < T; ++w) pool.emplace_back(chains, w);
+  for (auto& t : pool) t.join();
+  for (int w = 0; w < T; ++w)
+    for (size_t i = 0; i < films[w].size(); ++i) out[i] += films[w][i];
+  stats[1] = static_cast<double>(accepted.load());
   return 0;
 }
 
