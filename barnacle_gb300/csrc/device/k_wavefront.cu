@@ -99,50 +99,70 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
   }
 }
 
+// Persistent lanes with dynamic ray fetch: a lane whose ray finished claims the next queued ray
+// (one atomic per warp for all lanes that need one) and keeps stepping, so a warp never waits
+// out its slowest ray with idle lanes while work remains in the queue.
+__device__ __forceinline__ int fetch_next(int* counter, bool need) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, need);
+  if (!m) return -1;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(act, base, leader);
+  return need ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
 template <bool kWT>
 __global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
   const int n = p.counters[kCntActive];
-  const int stride = gridDim.x * blockDim.x;
-  const int nw = (n + 31) & ~31;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
-    const bool valid = i < n;
-    int bin = kBinMiss;
-    int slot = 0;
-    if (valid) {
-      slot = p.q_active[i];
+  int sn[kStackSize];
+  float st[kStackSize];
+  Trav tr;
+  TraceCounters tc;
+  int slot = -1;
+  bool need = true;
+  for (;;) {
+    const int qi = fetch_next(&p.counters[kCntFetchRay], need);
+    if (need) {
+      if (qi >= n) break;
+      slot = p.q_active[qi];
       const float4 o = p.ray_o[slot], d = p.ray_d[slot];
       Ray ray;
       ray.o = mk(o.x, o.y, o.z);
       ray.d = mk(d.x, d.y, d.z);
-      HitRec h;
-      TraceCounters tc;
-      if (trace_closest<kWT, false>(s, ray, CUDART_INF_F, &h, &tc)) {
-        p.hit_f[slot] = make_float4(h.t, h.u, h.v, 0.f);
-        p.hit_i[slot] = make_int2(h.inst, h.sphere_root ? h.sphere_root : h.tri);
-        const DevInstance* I = s.inst + h.inst;
-        int m = __ldg(&I->material);
-        if (m >= 0 && __ldg(&I->prim_type) == kPrimMesh) {
-          const int slot_m = __float_as_int(__ldg(&s.tris[3 * (__ldg(&I->tri_base) + h.tri)].w));
-          if (slot_m >= 0) m = slot_m;
-        }
-        bin = m < 0 ? kBinNoMaterial : s.mats[m].type;
-      } else {
-        p.hit_i[slot] = make_int2(-1, 0);
+      trav_init<false>(tr, s, ray, CUDART_INF_F, &tc);
+      need = false;
+    }
+    if (!trav_step<false, kWT, false>(tr, s, sn, st, &tc)) continue;
+    need = true;
+    int bin = kBinMiss;
+    if (tr.found) {
+      const HitRec& h = tr.hit;
+      p.hit_f[slot] = make_float4(h.t, h.u, h.v, 0.f);
+      p.hit_i[slot] = make_int2(h.inst, h.sphere_root ? h.sphere_root : h.tri);
+      const DevInstance* I = s.inst + h.inst;
+      int m = __ldg(&I->material);
+      if (m >= 0 && __ldg(&I->prim_type) == kPrimMesh) {
+        const int slot_m = __float_as_int(__ldg(&s.tris[3 * (__ldg(&I->tri_base) + h.tri)].w));
+        if (slot_m >= 0) m = slot_m;
       }
+      bin = m < 0 ? kBinNoMaterial : s.mats[m].type;
+    } else {
+      p.hit_i[slot] = make_int2(-1, 0);
     }
-    // material binning: lanes with equal keys share one atomic
-    const unsigned peers = __match_any_sync(0xffffffffu, valid ? bin : -1);
-    if (valid) {
-      const int leader = __ffs(peers) - 1;
-      const int lane = threadIdx.x & 31;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(&p.counters[kCntBin0 + bin], __popc(peers));
-      base = __shfl_sync(peers, base, leader);
-      const int pos = base + __popc(peers & ((1u << lane) - 1u));
-      p.q_bins[static_cast<long long>(bin) * p.pool + pos] = slot;
-    }
+    // material binning among the lanes finishing together: equal keys share one atomic
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, bin);
+    const int leader = __ffs(peers) - 1;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&p.counters[kCntBin0 + bin], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    p.q_bins[static_cast<long long>(bin) * p.pool + base + __popc(peers & ((1u << lane) - 1u))] = slot;
   }
 }
 
@@ -261,16 +281,30 @@ template <bool kWT>
 __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
-  const int stride = gridDim.x * blockDim.x;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const float4* r = p.shadow + 4LL * i;
-    const float4 o = r[0], d = r[1];
-    Ray ray;
-    ray.o = mk(o.x, o.y, o.z);
-    ray.d = mk(d.x, d.y, d.z);
-    TraceCounters tc;
-    if (!trace_any<kWT, false>(p.scene, ray, o.w, &tc)) {
-      const int slot = __float_as_int(d.w);
+  int sn[kStackSize];
+  float st[kStackSize];
+  Trav tr;
+  TraceCounters tc;
+  int rec = -1;
+  bool need = true;
+  for (;;) {
+    const int qi = fetch_next(&p.counters[kCntFetchShadow], need);
+    if (need) {
+      if (qi >= n) break;
+      rec = qi;
+      const float4* r = p.shadow + 4LL * rec;
+      const float4 o = r[0], d = r[1];
+      Ray ray;
+      ray.o = mk(o.x, o.y, o.z);
+      ray.d = mk(d.x, d.y, d.z);
+      trav_init<false>(tr, p.scene, ray, o.w, &tc);
+      need = false;
+    }
+    if (!trav_step<true, kWT, false>(tr, p.scene, sn, st, &tc)) continue;
+    need = true;
+    if (!tr.found) {
+      const float4* r = p.shadow + 4LL * rec;
+      const int slot = __float_as_int(r[1].w);
       const float4 a = r[2], b = r[3];
       float4 L = p.L[slot];
       L.x = fmaf(a.x, b.x, L.x);
@@ -293,6 +327,8 @@ __global__ void k_wf_control(WfParams* pp, int use_graph) {
   }
   c[kCntActive] = 0;
   c[kCntShadow] = 0;
+  c[kCntFetchRay] = 0;
+  c[kCntFetchShadow] = 0;
   c[kCntCont] = 0;
   c[kCntDone] = 0;
   for (int b = 0; b < kNumBins; ++b) c[kCntBin0 + b] = 0;

@@ -15,6 +15,8 @@ enum : int {
   kCntDone = 3,     // paths that ended this iteration (retired by the next regen)
   kCntIter = 4,     // iterations run
   kCntAgain = 5,    // last control decision (host-driven loop)
+  kCntFetchRay = 6, // dynamic-fetch cursors of the extend and shadow kernels
+  kCntFetchShadow = 7,
   kCntBin0 = 8,     // 8..13: per-bin hit counts
   kCntSize = 16
 };

@@ -122,7 +122,7 @@ def test_watertight_and_moller_trumbore_agree_off_edges(ctx, loaded):
     tie = np.abs(mt["t"] - wt["t"]) <= 1e-6 * np.maximum(mt["t"], wt["t"])
     assert (~same & far & tie).sum() > 0, "the Cornell boxes stand on the floor: ties are expected"
     assert (same | tie)[far].mean() > 0.9999, f"id mismatch rate {1 - (same | tie)[far].mean():.2e}"
-    both = same & (mt["instance"] >= 0)
+    both = same & (mt["instance"] >= 0) & far
     np.testing.assert_allclose(wt["t"][both], mt["t"][both], rtol=1e-5)
     both_hit = (mt["instance"] >= 0) & (wt["instance"] >= 0) & far
     np.testing.assert_allclose(wt["t"][both_hit], mt["t"][both_hit], rtol=1e-5)
