@@ -273,6 +273,7 @@ struct LightSample {
   V3 L;      // emitted radiance toward the shading point
   float pdf; // solid-angle pdf (includes the light choice)
   V3 wi;     // direction from the shading point to the light
+  int light; // index of the sampled light
 };
 
 // LightSamplerBase.Sample: UniformLightSampler.Sample (Uniform.fs:13-29) or the alias-table
@@ -326,6 +327,7 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& s, V3 p, flo
   ls.L = light_le(s.lights[light], dot(wo, sp.n));
   ls.pdf = __fdiv_rn(__fmul_rn(dist2, sp.pdf), __fmul_rn(fmaxf(fabsf(cos_wo), 1e-6f), sel));
   ls.wi = neg(wo);
+  ls.light = light;
   return ls;
 }
 

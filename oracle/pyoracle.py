@@ -35,6 +35,8 @@ def lib() -> C.CDLL:
             "or_bsdf": (C.c_int, [P, P, C.c_int64, C.c_int, C.c_int, P]),
             "or_render_pt": (C.c_int, [P, C.POINTER(capi.bn_render_desc), C.POINTER(capi.bn_view), C.c_int32,
                                        C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]),
+            "or_render_slots": (C.c_int, [P, C.POINTER(capi.bn_render_desc), C.POINTER(capi.bn_view), C.c_int32,
+                                          C.c_int32, P, P, C.c_int32, P]),
             "or_render_pssmlt": (C.c_int, [P, C.POINTER(capi.bn_render_desc), C.POINTER(capi.bn_view), C.c_int32,
                                            P, P, P]),
         }
@@ -124,3 +126,13 @@ class Scene:
         threads = threads or os.cpu_count() or 1
         lib().or_render_pssmlt(self._h, C.byref(desc), C.byref(view), threads, ptr(out), ptr(stats), ptr(boot))
         return out, float(stats[0]), int(stats[1]), int(stats[2]), boot
+
+    def render_slots(self, desc, view, n_slots, emissive_base, params, sparams=None, threads: int | None = None):
+        """Forward render with material slots from params (sampling from sparams, default params)."""
+        out = np.zeros((view.height, view.width, 3), np.float32)
+        prm = np.ascontiguousarray(params, np.float32)
+        sp = prm if sparams is None else np.ascontiguousarray(sparams, np.float32)
+        threads = threads or os.cpu_count() or 1
+        lib().or_render_slots(self._h, C.byref(desc), C.byref(view), n_slots, emissive_base, ptr(prm), ptr(sp),
+                              threads, ptr(out))
+        return out

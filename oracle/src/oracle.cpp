@@ -814,6 +814,7 @@ struct Scene {
     Vector3 p, L;
     float pdf;
     Vector3 wi;
+    int light;
   };
   // UniformLightSampler.Sample (Uniform.fs:13-29) or the alias-table sampler over triangles
   LightSample SampleLight(const Vector3& p, float uSelect, float ux, float uy) const {
@@ -856,6 +857,7 @@ struct Scene {
     ls.L = lights[light].Eval(f.WorldToLocal(wo));
     ls.pdf = dist2 * sp.pdf / (std::max(std::fabs(cosWo), 1e-6f) * sel);
     ls.wi = -wo;
+    ls.light = light;
     return ls;
   }
   // LightSamplerBase.Eval (Uniform.fs:40-49)
@@ -1360,6 +1362,102 @@ int or_render_pt(const or_scene* os, const bn_render_desc* d, const bn_view* vie
     for (const auto& c : per) { tot.rays += c.rays; tot.nodes += c.nodes; tot.tris += c.tris; tot.insts += c.insts; }
     counts[0] = tot.rays; counts[1] = tot.nodes; counts[2] = tot.tris; counts[3] = tot.insts;
   }
+  return 0;
+}
+
+// Differentiable-material forward (no reference counterpart): PathTracingIntegrator.Li where
+// material slots 0..emissive_base-1 are PBR materials built from `params` (values) and
+// `sparams` (sampling decisions: direction, pdf, MIS, RR), and light l's emission is scaled by
+// params[6 * (emissive_base + l) + 5].  With sparams == params this is the plain estimator.
+int or_render_slots(const or_scene* os, const bn_render_desc* d, const bn_view* view, int32_t n_slots,
+                    int32_t emissive_base, const float* params, const float* sparams, int32_t threads, float* out) {
+  const Scene& sc = *os->s;
+  const Camera cam = Camera::From(*view);
+  const int W = view->width, H = view->height;
+  auto slot_mat = [&](const float* prm, int s) {
+    bn_material_desc md{};
+    md.type = BN_MAT_PBR;
+    md.base_color[0] = prm[6 * s]; md.base_color[1] = prm[6 * s + 1]; md.base_color[2] = prm[6 * s + 2];
+    md.roughness = prm[6 * s + 3];
+    md.metallic = prm[6 * s + 4];
+    md.ior = 1.5f;
+    return MaterialF::From(md);
+  };
+  auto scale_of = [&](int light) {
+    const int s = emissive_base + light;
+    return (light >= 0 && s < n_slots) ? params[6 * s + 5] : 1.f;
+  };
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    Counters c;
+    for (;;) {
+      const int row = next.fetch_add(1);
+      if (row >= H) break;
+      const int y = row;
+      for (int x = 0; x < W; ++x) {
+        Vector3 acc(0.f);
+        const float invSpp = 1.f / static_cast<float>(d->spp);
+        for (int si = 0; si < d->spp; ++si) {
+          IndepSampler smp{Sampler::Three(static_cast<uint32_t>(x), static_cast<uint32_t>(y),
+                                           static_cast<uint32_t>(d->frame_id * d->spp + si))};
+          const float upx = smp.next(), upy = smp.next(), ulx = smp.next(), uly = smp.next();
+          Ray ray = cam.Generate(x, y, upx, upy, ulx, uly);
+          Vector3 L(0.f), beta(1.f), beta_s(1.f);
+          float pdfB = 0.f;
+          int depth = 0;
+          while (depth < d->max_depth) {
+            float t = kInf;
+            Interaction it;
+            if (!sc.Closest(ray, &t, &it, false, &c)) break;
+            const Instance& I = sc.inst[it.inst];
+            if (I.light >= 0) {
+              Vector3 le;
+              float pdfL;
+              sc.EvalLight(ray.Origin, it, &le, &pdfL);
+              const float mis = depth == 0 ? 1.f : pdfB * (1.f / (pdfL + pdfB));
+              L = Vector3::FusedMultiplyAdd(beta, (scale_of(I.light) * le) * mis, L);
+            }
+            const int mat = sc.HitMaterial(it);
+            if (mat < 0) break;
+            const float uSel = smp.next(), ulx2 = smp.next(), uly2 = smp.next();
+            const bool slotted = mat < emissive_base && mat < n_slots;
+            const MaterialF ms = slotted ? slot_mat(sparams, mat) : sc.mats[mat];
+            const MaterialF mv = slotted ? slot_mat(params, mat) : ms;
+            const Vector3 wo = it.geom.onb.WorldToLocal(-ray.Direction);
+            const Scene::LightSample ls = sc.SampleLight(it.geom.p, uSel, ulx2, uly2);
+            const float dist = (ls.p - it.geom.p).Length();
+            if (ls.pdf != 0.f && !sc.Any(Ray{it.geom.p, ls.wi}, dist - 1e-3f, false, &c)) {
+              const Vector3 wi = it.geom.onb.WorldToLocal(ls.wi);
+              const BSDFEvalT<float> bes = ms.Eval(wo, wi);
+              const BSDFEvalT<float> bev = slotted ? mv.Eval(wo, wi) : bes;
+              const Vector3 leV = scale_of(ls.light) * ls.L;
+              L = Vector3::FusedMultiplyAdd(beta * bev.bsdf, leV * (1.f / (bes.pdf + ls.pdf)), L);
+            }
+            const float uLobe = smp.next(), ubx = smp.next(), uby = smp.next();
+            const BSDFSampleT<float> bs = ms.Sample(wo, uLobe, ubx, uby);
+            if (bs.eval.pdf == 0.f) break;
+            const Vector3 fv = slotted ? mv.Eval(wo, bs.wi).bsdf : bs.eval.bsdf;
+            pdfB = bs.eval.pdf;
+            ray = {it.geom.p, it.geom.onb.LocalToWorld(bs.wi)};
+            beta = beta * fv * (1.f / bs.eval.pdf);
+            beta_s = beta_s * bs.eval.bsdf * (1.f / bs.eval.pdf);
+            if (depth >= d->rr_depth) {
+              const float q = MathMin(1.f, MathMax(beta_s.X, MathMax(beta_s.Y, beta_s.Z)));
+              if (smp.next() < q) { beta = beta * (1.f / q); beta_s = beta_s * (1.f / q); }
+              else break;
+            }
+            depth++;
+          }
+          acc = Vector3::FusedMultiplyAdd(Vector3(invSpp), L, acc);
+        }
+        const size_t idx = static_cast<size_t>(H - y - 1) * W + x;
+        out[3 * idx] = acc.X; out[3 * idx + 1] = acc.Y; out[3 * idx + 2] = acc.Z;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 0; w < std::max(threads, 1); ++w) pool.emplace_back(worker);
+  for (auto& t : pool) t.join();
   return 0;
 }
 

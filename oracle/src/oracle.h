@@ -23,6 +23,8 @@ int or_bsdf(const bn_material_desc* materials, const bn_bsdf_query* q, int64_t n
             double* out7);
 int or_render_pt(const or_scene* s, const bn_render_desc* d, const bn_view* view, int32_t x0, int32_t y0, int32_t x1,
                  int32_t y1, int32_t threads, float* out, uint64_t* counts);
+int or_render_slots(const or_scene* s, const bn_render_desc* d, const bn_view* view, int32_t n_slots,
+                    int32_t emissive_base, const float* params, const float* sparams, int32_t threads, float* out);
 int or_render_pssmlt(const or_scene* s, const bn_render_desc* d, const bn_view* view, int32_t threads, float* out,
                      double* stats, float* bootstrap_out);
 
