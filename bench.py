@@ -151,6 +151,73 @@ def cpu_sample_render(bundle, render, spp, views, crop_size, threads):
     return paths, secs
 
 
+def run_extras(ctx, args, torch, flush):
+    """The other parts of the metric, each on its own workload (device-timed, L2 flushed first):
+    the Cornell box (256^2, 64 spp, depth 8) against the CPU path on this host; PSSMLT (1024^2,
+    2^20 bootstrap paths, 65,536 chains, 16 mutations per pixel, Kelemen(1/1024, 1/64), depth 16);
+    adjoint / forward cost on the 32-slot material workload (256^2, 16 spp, depth 8)."""
+    from barnacle_gb300 import Bundle, capi
+    from barnacle_gb300.inverse import MaterialProblem
+
+    out = {}
+    # Cornell box: plain megakernel vs the CPU restatement (same workload, bounded CPU sample)
+    c0 = Bundle.generate("cornell", 1)
+    ctx.upload(c0)
+    r0 = c0.render
+    r0.mode = capi.BN_MODE_MEGAKERNEL
+    v0 = c0.views
+    for k in range(3):
+        r0.frame_id = k
+        ctx.render(r0, v0, to_host=False)
+    ms = []
+    for k in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r0.frame_id = 10 + k
+        ctx.render(r0, v0, to_host=False)
+        ms.append(ctx.stats().last_kernel_ms)
+    paths0 = v0[0].width * v0[0].height * r0.spp
+    gpu0 = paths0 / (min(ms) / 1000.0)
+    threads = os.cpu_count() or 1
+    pc, sc = cpu_sample_render(c0, c0.render, 64, v0, 96, threads)
+    out["cornell"] = {"gpu_paths_per_s": gpu0, "gpu_ms": min(ms), "cpu_paths_per_s": pc / sc, "cpu_cores": threads,
+                      "cpu_sample": "96x96 centre crop x 64 spp", "gpu_over_cpu": gpu0 / (pc / sc)}
+    # PSSMLT
+    c3 = Bundle.generate("pssmlt", 1)
+    ctx.upload(c3)
+    r3 = c3.render
+    r3.frame_id = 0
+    ctx.render(r3, c3.views, to_host=False)
+    flush.zero_()
+    torch.cuda.synchronize()
+    ctx.reset_stats()
+    r3.frame_id = 1
+    ctx.render(r3, c3.views, to_host=False)
+    st = ctx.stats()
+    out["pssmlt"] = {"ms": st.last_kernel_ms, "chain_ms": st.last_dominant_ms,
+                     "proposals_per_s": st.proposed / (st.last_dominant_ms / 1000.0),
+                     "paths_per_s": st.paths / (st.last_kernel_ms / 1000.0),
+                     "acceptance": st.accepted / max(1, st.proposed), "b": st.bootstrap_b}
+    # adjoint / forward
+    c4 = Bundle.generate("materials", 1)
+    pb = MaterialProblem(ctx, c4, width=256, height=256, spp=16, max_depth=8)
+    target = pb.render(c4.slot_params(), spp=16, frame=1)
+    theta = pb.random_params(2)
+    fwd, bwd = [], []
+    for k in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        pb.render(theta, frame=2 + k)
+        fwd.append(ctx.stats().last_kernel_ms)
+        flush.zero_()
+        torch.cuda.synchronize()
+        pb.loss_and_grad(theta, target, frame=2 + k)
+        bwd.append(ctx.stats().last_kernel_ms)
+    out["adjoint"] = {"forward_ms": min(fwd), "backward_ms": min(bwd), "backward_over_forward": min(bwd) / min(fwd),
+                      "workload": "materials 256^2 x 16 spp, depth 8, 32 slots (forward + loss + replay)"}
+    return out
+
+
 def run_reference(args, world, rank, dist):
     """--impl reference: the CPU restatement on all host threads, bounded samples per step."""
     if rank != 0:
@@ -195,6 +262,8 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other render form")
     ap.add_argument("--spp-per-step", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the Cornell-box CPU ratio, PSSMLT and adjoint/forward measurements")
     ap.add_argument("--no-graph", action="store_true",
                     help="wavefront bounce loop driven from the host (ncu cannot profile kernels inside a "
                          "graph with a conditional node)")
@@ -291,10 +360,14 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        p, s = cpu_sample_render(b, b.render, args.spp_per_step, views[:4], 48, threads)
+        p, s = cpu_sample_render(b, b.render, 24, views[:4], 128, threads)
         cpu = {"value": p / s, "unit": "paths/s", "cores": threads, "kind": "port",
-               "sample": f"48x48 centre crops of 4 of the 16 views x {args.spp_per_step} spp "
+               "sample": "128x128 centre crops of 4 of the 16 views x 24 spp "
                          "(oracle: CPU restatement of the F# path; the F# renderer cannot be built here)"}
+
+    extras = None
+    if rank == 0 and not args.no_extras:
+        extras = run_extras(ctx, args, torch, flush)
 
     if rank == 0:
         value = world * paths_per_step * args.steps / dev_s
@@ -329,6 +402,7 @@ def main():
                 "equal_rmse": "same per-path estimator and random streams in both forms (images equal to "
                               "float summation order, tests/test_gpu_wavefront.py)"},
             "wall_s": wall,
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

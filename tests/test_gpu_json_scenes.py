@@ -1,0 +1,93 @@
+"""Scenes read through the reference's JSON schema (bn_bundle_load_json), rendered on the device and
+checked against the oracle: analytic spheres (SpherePrimitive.Intersect), the thin-lens camera,
+an emissive sphere (SphereInstance.Sample / EvalPDF with the uniform light sampler), PSSMLT with
+the loader's Kelemen settings."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from barnacle_gb300 import Bundle, capi
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+SCENES = Path(__file__).resolve().parent / "golden" / "scenes"
+
+
+def scene_rays(n, lo, hi, eye, rng):
+    r = np.zeros(2 * n, capi.RAY_DTYPE)
+    r["origin"][:n] = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    r["origin"][n:] = eye
+    tgt = rng.uniform(lo, hi, size=(2 * n, 3)).astype(np.float32)
+    d = np.where(np.arange(2 * n)[:, None] < n, rng.normal(size=(2 * n, 3)), tgt - eye).astype(np.float32)
+    r["direction"] = d / np.sqrt((d ** 2).sum(1, dtype=np.float32))[:, None]
+    r["t_max"] = np.inf
+    return r
+
+
+@pytest.mark.parametrize("name,lo,hi", [("spheres_thinlens.json", (0, 0, 0), (100, 90, 250)),
+                                         ("sphere_light.json", (-5, 0, -5), (5, 5, 5))])
+def test_json_scene_trace_bit_exact(ctx, name, lo, hi):
+    b = Bundle.load_json(str(SCENES / name))
+    ctx.upload(b)
+    o = pyoracle.Scene(b.scene)
+    eye = np.array(list(b.views[0].camera.camera_to_world)[12:15], np.float32)
+    rays = scene_rays(8000, lo, hi, eye, np.random.default_rng(2))
+    for flags in (0, capi.BN_TRACE_WATERTIGHT):
+        g = ctx.trace(rays, flags)
+        h, _ = o.trace(rays, flags)
+        assert (h["instance"] >= 0).mean() > 0.2
+        assert np.array_equal(g["instance"], h["instance"]) and np.array_equal(g["primitive"], h["primitive"])
+        hit = h["instance"] >= 0
+        assert np.array_equal(g["t"][hit].view(np.uint32), h["t"][hit].view(np.uint32))
+        assert np.array_equal(g["u"][hit].view(np.uint32), h["u"][hit].view(np.uint32))
+    rays["t_max"] = np.random.default_rng(3).uniform(0.1, 50, len(rays)).astype(np.float32)
+    g = ctx.trace(rays, capi.BN_TRACE_ANY)
+    h, _ = o.trace(rays, capi.BN_TRACE_ANY)
+    assert np.array_equal(g["instance"] >= 0, h["instance"] >= 0)
+
+
+@pytest.mark.parametrize("name,mode", [("sphere_light.json", capi.BN_MODE_MEGAKERNEL),
+                                        ("sphere_light.json", capi.BN_MODE_WAVEFRONT),
+                                        ("spheres_thinlens.json", capi.BN_MODE_MEGAKERNEL)])
+def test_json_scene_render_matches_oracle(ctx, name, mode):
+    b = Bundle.load_json(str(SCENES / name))
+    ctx.upload(b)
+    o = pyoracle.Scene(b.scene)
+    r = b.render
+    r.integrator = capi.BN_INTEGRATOR_PATH
+    r.mode = mode
+    r.spp = 16
+    v = b.views[0]
+    gpu, cpu = [], []
+    for f in range(10):
+        r.frame_id = f
+        gpu.append(ctx.render(r, v)[0].astype(np.float64))
+        r.frame_id = 500 + f
+        cpu.append(o.render_pt(r, v)[0].astype(np.float64))
+    g, c = np.stack(gpu), np.stack(cpu)
+    mg, mc = g.mean(0), c.mean(0)
+    se = np.sqrt(g.var(0, ddof=1) / len(g) + c.var(0, ddof=1) / len(c))
+    valid = se > 0
+    z = np.abs(mg - mc)[valid] / se[valid]
+    assert (z > 3).mean() < 0.02, f"{(z > 3).mean():.3%} of pixel means beyond 3 standard errors"
+    assert abs(mg.mean() / mc.mean() - 1) < 0.03
+
+
+def test_json_scene_pssmlt_matches_oracle(ctx):
+    b = Bundle.load_json(str(SCENES / "spheres_thinlens.json"))
+    ctx.upload(b)
+    o = pyoracle.Scene(b.scene)
+    r = b.render
+    assert r.integrator == capi.BN_INTEGRATOR_PSSMLT and r.mutation == capi.BN_MUTATION_KELEMEN
+    r.flags = capi.BN_RENDER_FIXED_ALIAS
+    r.spp = 16
+    v = b.views[0]
+    ctx.reset_stats()
+    gi = ctx.render(r, v)[0]
+    st = ctx.stats()
+    ci, cb, acc, prop, _ = o.render_pssmlt(r, v)
+    assert np.isfinite(gi).all() and np.isfinite(ci).all()
+    assert abs(st.bootstrap_b / cb - 1) < 0.05
+    assert abs(st.accepted / acc - 1) < 0.05 and st.proposed == prop
+    assert abs(gi.sum() / ci.sum() - 1) < 0.05
