@@ -33,6 +33,10 @@ def test_json_scene_trace_bit_exact(ctx, name, lo, hi):
     o = pyoracle.Scene(b.scene)
     eye = np.array(list(b.views[0].camera.camera_to_world)[12:15], np.float32)
     rays = scene_rays(8000, lo, hi, eye, np.random.default_rng(2))
+    s = b.scene.contents
+    order = ctx.instance_order(s.n_instances)
+    is_sphere = np.array([s.primitives[s.instances[order[k]].primitive].type == capi.BN_PRIM_SPHERE
+                          for k in range(s.n_instances)])
     for flags in (0, capi.BN_TRACE_WATERTIGHT):
         g = ctx.trace(rays, flags)
         h, _ = o.trace(rays, flags)
@@ -40,7 +44,14 @@ def test_json_scene_trace_bit_exact(ctx, name, lo, hi):
         assert np.array_equal(g["instance"], h["instance"]) and np.array_equal(g["primitive"], h["primitive"])
         hit = h["instance"] >= 0
         assert np.array_equal(g["t"][hit].view(np.uint32), h["t"][hit].view(np.uint32))
-        assert np.array_equal(g["u"][hit].view(np.uint32), h["u"][hit].view(np.uint32))
+        sph = hit & is_sphere[np.maximum(h["instance"], 0)]
+        tri = hit & ~sph
+        assert sph.sum() > 100 and tri.sum() > 100
+        # triangle barycentrics are exact arithmetic; the sphere uv map goes through atan2/acos,
+        # whose last bit differs between CUDA's and the C library's implementations
+        for f in ("u", "v"):
+            assert np.array_equal(g[f][tri].view(np.uint32), h[f][tri].view(np.uint32))
+            np.testing.assert_allclose(g[f][sph], h[f][sph], rtol=1e-6, atol=1e-7)
     rays["t_max"] = np.random.default_rng(3).uniform(0.1, 50, len(rays)).astype(np.float32)
     g = ctx.trace(rays, capi.BN_TRACE_ANY)
     h, _ = o.trace(rays, capi.BN_TRACE_ANY)
