@@ -100,11 +100,10 @@ __device__ __forceinline__ bool box_hit(V3 bmin, V3 bmax, const Ray& r, V3 inv, 
   const float t0x = __fmul_rn(__fsub_rn(bmin.x, r.o.x), inv.x), t1x = __fmul_rn(__fsub_rn(bmax.x, r.o.x), inv.x);
   const float t0y = __fmul_rn(__fsub_rn(bmin.y, r.o.y), inv.y), t1y = __fmul_rn(__fsub_rn(bmax.y, r.o.y), inv.y);
   const float t0z = __fmul_rn(__fsub_rn(bmin.z, r.o.z), inv.z), t1z = __fmul_rn(__fsub_rn(bmax.z, r.o.z), inv.z);
-  const float lx = t0x < t1x ? t0x : t1x, hx = t0x > t1x ? t0x : t1x;
-  const float ly = t0y < t1y ? t0y : t1y, hy = t0y > t1y ? t0y : t1y;
-  const float lz = t0z < t1z ? t0z : t1z, hz = t0z > t1z ? t0z : t1z;
-  const float tmin = fmaxf(1e-3f, fmaxf(lx, fmaxf(ly, lz)));
-  const float tmax = fminf(tmax_in, fminf(hx, fminf(hy, hz)));
+  // fminf/fmaxf decide exactly as MinNative/MaxNative would: they differ only for a NaN t1,
+  // which the NaN check below rejects, and zero signs cannot change the comparison
+  const float tmin = fmaxf(1e-3f, fmaxf(fminf(t0x, t1x), fmaxf(fminf(t0y, t1y), fminf(t0z, t1z))));
+  const float tmax = fminf(tmax_in, fminf(fmaxf(t0x, t1x), fminf(fmaxf(t0y, t1y), fmaxf(t0z, t1z))));
   const bool nan = (t1x != t1x) | (t1y != t1y) | (t1z != t1z);
   return (tmin <= tmax) & !nan;
 }

@@ -137,7 +137,8 @@ __global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ 
       trav_init<false>(tr, s, ray, CUDART_INF_F, &tc);
       need = false;
     }
-    if (!trav_step<false, kWT, false>(tr, s, sn, st, &tc)) continue;
+    // a walk can end at init (root box missed)
+    if (tr.mode != kTravDone && !trav_step<false, kWT, false>(tr, s, sn, st, &tc)) continue;
     need = true;
     int bin = kBinMiss;
     if (tr.found) {
@@ -300,7 +301,8 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ 
       trav_init<false>(tr, p.scene, ray, o.w, &tc);
       need = false;
     }
-    if (!trav_step<true, kWT, false>(tr, p.scene, sn, st, &tc)) continue;
+    if (tr.mode != kTravDone && !trav_step<true, kWT, false>(tr, p.scene, sn, st, &tc))
+      continue;
     need = true;
     if (!tr.found) {
       const float4* r = p.shadow + 4LL * rec;

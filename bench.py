@@ -264,6 +264,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the Cornell-box CPU ratio, PSSMLT and adjoint/forward measurements")
+    ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0 = autotuned)")
+    ap.add_argument("--cap", type=int, default=0, help="wavefront blocks per SM cap (0 = autotuned)")
     ap.add_argument("--no-graph", action="store_true",
                     help="wavefront bounce loop driven from the host (ncu cannot profile kernels inside a "
                          "graph with a conditional node)")
@@ -285,6 +287,8 @@ def main():
     r.spp = args.spp_per_step
     if args.no_graph:
         r.flags |= capi.BN_RENDER_NO_GRAPH
+    r.queue_capacity = args.pool
+    r.block_size = args.cap
     pixels = sum(v.width * v.height for v in views)
     paths_per_step = pixels * r.spp
     torch.cuda.set_device(dev)
