@@ -25,6 +25,7 @@ BN_PRIM_MESH, BN_PRIM_SPHERE = 0, 1
 BN_MAT_LAMBERTIAN, BN_MAT_MIRROR, BN_MAT_DIELECTRIC, BN_MAT_PBR = 0, 1, 2, 3
 BN_CAM_PINHOLE, BN_CAM_THIN_LENS = 0, 1
 BN_LIGHTS_UNIFORM, BN_LIGHTS_ALIAS_TRIANGLES = 0, 1
+BN_BVH_AUTO, BN_BVH_BINARY, BN_BVH_WIDE = 0, 2, 4
 BN_TRACE_CLOSEST, BN_TRACE_ANY, BN_TRACE_WATERTIGHT, BN_TRACE_COUNT = 0x0, 0x1, 0x2, 0x4
 BN_INTEGRATOR_PATH, BN_INTEGRATOR_PSSMLT = 0, 1
 BN_MODE_MEGAKERNEL, BN_MODE_WAVEFRONT = 0, 1
@@ -68,7 +69,7 @@ class bn_scene_desc(C.Structure):
                 ("instances", C.POINTER(bn_instance_desc)), ("n_instances", C.c_int32),
                 ("materials", C.POINTER(bn_material_desc)), ("n_materials", C.c_int32),
                 ("lights", C.POINTER(bn_light_desc)), ("n_lights", C.c_int32),
-                ("light_sampler", C.c_int32)]
+                ("light_sampler", C.c_int32), ("bvh_width", C.c_int32)]
 
 
 class bn_ray(C.Structure):

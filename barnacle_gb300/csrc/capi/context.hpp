@@ -40,7 +40,7 @@ struct bn_context {
   // scene
   bool has_scene = false;
   bn::DevScene scene{};
-  DevBuf nodes, tris, inst, mats, lights, light_inst, tri_pdf, tri_lights, error_word, counters;
+  DevBuf nodes, nodes4, tris, inst, mats, lights, light_inst, tri_pdf, tri_lights, error_word, counters;
   std::vector<int32_t> inst_order;     // TLAS order -> descriptor index
   std::vector<bn::DevMaterial> host_mats;
   std::vector<int32_t> host_inst_light;  // per TLAS instance: light index

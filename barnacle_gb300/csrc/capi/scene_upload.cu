@@ -48,7 +48,82 @@ void columns(const float* m, float4 out[3]) {
 struct MeshPrep {
   std::vector<bn_bvh_node> nodes;
   std::vector<int32_t> perm;
-  int node_base = 0, tri_base = 0;
+  int node_base = 0, tri_base = 0, node4_root = -1;
+};
+
+// The wide records of one binary BVH (layout in dev_types.cuh).  A record stands for an
+// interior node g and holds the boxes the reference tests in the two steps below g: g's
+// children's children, or a child itself when it is a leaf.  The walk over records makes the
+// binary walk's decisions because a box nested in another is never entered when the outer one
+// is not: slab distances are monotone in the box planes under round-to-nearest (and a zero
+// direction component admits exactly the boxes whose open slab holds the origin), so testing a
+// grandchild alone gives the answer of testing it after its parent with the same t.  That
+// needs every child box to contain its children's boxes, which the builder's unions guarantee
+// for finite bounds; the check below rejects the rest (NaN coordinates).
+struct Collapse {
+  const std::vector<bn_bvh_node>& b;
+  std::vector<float4>& out;
+  bool nested = true;
+
+  static bool inside(const bn_bvh_node& in, const bn_bvh_node& outer) {
+    for (int a = 0; a < 3; ++a)
+      if (!(outer.bounds_min[a] <= in.bounds_min[a] && in.bounds_max[a] <= outer.bounds_max[a])) return false;
+    return true;
+  }
+
+  int emit(int g) {
+    const int idx = static_cast<int>(out.size() / 8);
+    out.resize(out.size() + 8);
+    const int kids[2] = {g + 1, b[g].right_or_offset};
+    int slot[4] = {-1, -1, -1, -1};
+    int axis[3] = {b[g].split_axis, 0, 0};
+    for (int c = 0; c < 2; ++c) {
+      const bn_bvh_node& k = b[kids[c]];
+      if (k.is_leaf) {
+        slot[2 * c] = kids[c];
+      } else {
+        slot[2 * c] = kids[c] + 1;
+        slot[2 * c + 1] = k.right_or_offset;
+        axis[1 + c] = k.split_axis;
+        nested = nested && inside(b[kids[c] + 1], k) && inside(b[k.right_or_offset], k);
+      }
+    }
+    const float nan = std::numeric_limits<float>::quiet_NaN();
+    float box[6][4];
+    int ref[4] = {0, 0, 0, 0};
+    unsigned counts = 0, leaf_mask = 0;
+    for (int s = 0; s < 4; ++s) {
+      if (slot[s] < 0) {
+        for (int r = 0; r < 6; ++r) box[r][s] = nan;
+        continue;
+      }
+      const bn_bvh_node& n = b[slot[s]];
+      for (int a = 0; a < 3; ++a) {
+        box[a][s] = n.bounds_min[a];
+        box[3 + a][s] = n.bounds_max[a];
+      }
+      if (n.is_leaf) {
+        ref[s] = n.right_or_offset;
+        counts |= static_cast<unsigned>(static_cast<uint8_t>(n.count)) << (8 * s);
+        leaf_mask |= 1u << s;
+      } else {
+        ref[s] = emit(slot[s]);  // grows out: the record is written by index below
+      }
+    }
+    float4* r = &out[8 * static_cast<size_t>(idx)];
+    for (int k = 0; k < 6; ++k) r[k] = make_float4(box[k][0], box[k][1], box[k][2], box[k][3]);
+    float4 rf, mt;
+    std::memcpy(&rf, ref, 16);
+    const int meta[4] = {static_cast<int>(counts),
+                         static_cast<int>(leaf_mask | (static_cast<unsigned>(axis[0] & 3) << 4) |
+                                          (static_cast<unsigned>(axis[1] & 3) << 6) |
+                                          (static_cast<unsigned>(axis[2] & 3) << 8)),
+                         0, 0};
+    std::memcpy(&mt, meta, 16);
+    r[6] = rf;
+    r[7] = mt;
+    return idx;
+  }
 };
 
 // Vose's alias method over non-negative weights (double precision build)
@@ -214,6 +289,28 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   for (size_t k = 0; k < tlas.size(); ++k) put_node(&nodes[2 * k], tlas[k]);
   for (int i = 0; i < d->n_meshes; ++i)
     for (size_t k = 0; k < mp[i].nodes.size(); ++k) put_node(&nodes[2 * (n_tlas + mp[i].node_base + k)], mp[i].nodes[k]);
+  // wide records for every BVH with an interior root (the TLAS's first, at record 0) when the
+  // scene is walked wide: asked for, or automatically for scenes of 1,024+ nodes
+  if (d->bvh_width != BN_BVH_AUTO && d->bvh_width != BN_BVH_BINARY && d->bvh_width != BN_BVH_WIDE)
+    return ctx->fail(BN_ERR_INVALID_ARG, "bvh_width must be 0 (auto), 2 or 4");
+  const bool scene_wide = d->bvh_width == BN_BVH_WIDE || (d->bvh_width == BN_BVH_AUTO && nodes.size() / 2 >= 1024);
+  std::vector<float4> nodes4;
+  bool nested = true;
+  if (scene_wide && !tlas[0].is_leaf) {
+    Collapse c{tlas, nodes4};
+    c.emit(0);
+    nested = nested && c.nested;
+  }
+  for (int i = 0; i < d->n_meshes; ++i) {
+    if (!scene_wide || mp[i].nodes[0].is_leaf) continue;
+    Collapse c{mp[i].nodes, nodes4};
+    mp[i].node4_root = c.emit(0);
+    nested = nested && c.nested;
+  }
+  if (!nested) return ctx->fail(BN_ERR_INVALID_ARG, "non-finite triangle or instance bounds");
+  if (nodes4.size() / 8 >= (size_t{1} << 29))  // a stacked leaf slot is -1 - (4 * record + slot)
+    return ctx->fail(BN_ERR_UNSUPPORTED, "scene too large for the wide BVH records");
+  if (nodes4.empty()) nodes4.resize(8);  // keep the buffer non-null
 
   std::vector<bn::DevInstance> dinst(ni);
   std::vector<int32_t> inst_light(ni);
@@ -233,7 +330,7 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
     di.material = in.material;
     di.light = in.light;
     di.light_entry_base = -1;
-    di.mesh = p.type == BN_PRIM_MESH ? p.mesh : -1;
+    di.node4_root = p.type == BN_PRIM_MESH ? mp[p.mesh].node4_root : -1;
     inst_light[k] = in.light;
   }
 
@@ -306,6 +403,7 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   cudaStream_t st = ctx->stream;
   cudaError_t e;
   if ((e = upload(ctx->nodes, nodes, st)) != cudaSuccess) return ctx->cuda_fail(e, "upload nodes");
+  if ((e = upload(ctx->nodes4, nodes4, st)) != cudaSuccess) return ctx->cuda_fail(e, "upload wide nodes");
   if ((e = upload(ctx->tris, tris, st)) != cudaSuccess) return ctx->cuda_fail(e, "upload triangles");
   if ((e = upload(ctx->inst, dinst, st)) != cudaSuccess) return ctx->cuda_fail(e, "upload instances");
   if ((e = upload(ctx->mats, mats, st)) != cudaSuccess) return ctx->cuda_fail(e, "upload materials");
@@ -317,6 +415,7 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
 
   bn::DevScene& s = ctx->scene;
   s.nodes = ctx->nodes.as<float4>();
+  s.nodes4 = ctx->nodes4.as<float4>();
   s.tris = ctx->tris.as<float4>();
   s.inst = ctx->inst.as<bn::DevInstance>();
   s.mats = ctx->mats.as<bn::DevMaterial>();
@@ -327,6 +426,8 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   s.n_inst = ni;
   s.n_tlas_nodes = n_tlas;
   s.n_nodes = static_cast<int>(nodes.size() / 2);
+  s.n_nodes4 = static_cast<int>(nodes4.size() / 8);
+  s.wide = scene_wide ? 1 : 0;
   s.n_tris = static_cast<int>(tris.size() / 3);
   s.n_light_inst = static_cast<int>(light_inst.size());
   s.n_tri_lights = static_cast<int>(tl.size());

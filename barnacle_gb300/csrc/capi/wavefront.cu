@@ -112,8 +112,9 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   if ((e = w->film_acc.reserve(static_cast<size_t>(n_pixels) * 3 * sizeof(double))) != cudaSuccess)
     return ctx->cuda_fail(e, "wavefront film allocation");
   const bool wt = d->flags & BN_RENDER_WATERTIGHT;
-  if (w->shape_cap != cap || w->shape.watertight != wt) {
-    w->shape = bn::wf_launch_shape(wt, cap);
+  const bool wide = ctx->scene.wide != 0;
+  if (w->shape_cap != cap || w->shape.watertight != wt || w->shape.wide != wide) {
+    w->shape = bn::wf_launch_shape(wt, wide, cap);
     w->shape_cap = cap;
     if (w->exec) {
       cudaGraphExecDestroy(w->exec);

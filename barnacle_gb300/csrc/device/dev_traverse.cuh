@@ -3,22 +3,30 @@
 // Order and culling are the reference's (Aggregate/BVH.fs:11-58, Primitive.fs:111-129,
 // Mesh.fs:188-242): near child first (left when d[axis] > 0), the instances of a TLAS leaf in
 // order, each instance's BLAS walked completely before the next, every box tested against the
-// current t with tMin = 1e-3.  Two changes of form keep the SIMT lanes together:
-//  * an interior node tests both children at once (their four 16-byte halves load together),
-//    enters the near one and pushes the far one with its entry distance; on pop the far child is
-//    entered only if that distance is still <= t, which is exactly the reference's box test at
-//    pop time (a box that passed with a larger t passes with the current t iff its entry
-//    distance is <= t).  Closest-hit visit counts equal the reference's: the root plus both
-//    children of every entered interior node.
-//  * the walk is a flat state machine: each step is one bounded unit of work (a node pair, one
-//    triangle or one instance) at either BVH level, with pops folded into the step that needs
-//    them, so lanes at different levels run the same loop body and reconverge after every step
-//    instead of waiting out each other's nested BLAS loops.  A caller can refill a lane with a new
-//    ray as soon as its walk finishes.
+// current t with tMin = 1e-3.  Changes of form keep the SIMT lanes together and the loads few:
+//  * an interior node tests its children at once, enters the near one and pushes the far one
+//    with its entry distance; on pop the far child is entered only if that distance is still
+//    <= t, which is exactly the reference's box test at pop time (a box that passed with a
+//    larger t passes with the current t iff its entry distance is <= t).
+//  * the wide walk reads one 128-byte record per step that holds the two binary levels below
+//    the node (its grandchildren, see dev_types.cuh) and tests the four boxes together.  It
+//    visits them in the binary walk's order (near child's near child first, by the split axes
+//    of the node and of each child) and stacks the hits that pass so that they pop in that
+//    order.  Because a nested box passes whenever its parent box would with the same t, it
+//    visits the same leaves in the same order with the same t as the binary walk.  A scene is
+//    walked wide (kWalkWide) when the upload built records for it (large scenes; small BVHs gain
+//    nothing from them).  The counting walk (kWalkCount) is always the binary one, so its counts
+//    equal the reference's (the root plus both children of every entered interior node).
+//  * the walk is a flat state machine: each step is one bounded unit of work (a node record,
+//    one triangle or one instance) at either BVH level, with pops folded into the step that
+//    needs them, so lanes at different levels run the same loop body and reconverge after every
+//    step instead of waiting out each other's nested BLAS loops.  A caller can refill a lane
+//    with a new ray as soon as its walk finishes.
 
 namespace bn {
 
-constexpr int kStackSize = 136;  // TLAS and BLAS far-child entries of a depth-64 BVH pair
+// far entries of a depth-64 TLAS and BLAS: the wide walk stacks up to three per record level
+constexpr int kStackSize = 200;
 
 // the slab test that also reports the entry distance max(1e-3, t0') used by the pop check
 __device__ __forceinline__ bool box_hit_t(V3 bmin, V3 bmax, const Ray& r, V3 inv, float tmax_in, float* tentry) {
@@ -72,8 +80,27 @@ __device__ __forceinline__ void trav_enter(Trav& tr, int cur, const NodeRec& n) 
   }
 }
 
+// a leaf's item range: instances at the TLAS level, triangles at the BLAS level
+__device__ __forceinline__ void trav_enter_leaf(Trav& tr, int first, int count) {
+  if (tr.level == 0) {
+    tr.ii = first;
+    tr.ii_end = first + count;
+    tr.mode = kTravInst;
+  } else {
+    tr.ti = first;
+    tr.ti_end = first + count;
+    tr.mode = kTravTri;
+  }
+}
+
+__device__ __forceinline__ const float4* node4_at(const DevScene& s, int i) {
+  return s.nodes4 + 8 * static_cast<size_t>(i);
+}
+
 // the next stacked node still within reach; an exhausted BLAS returns to the instances of its
-// TLAS leaf, an exhausted TLAS ends the walk
+// TLAS leaf, an exhausted TLAS ends the walk.  Binary entries are node indices within the level;
+// wide entries are record indices (>= 0) or -1 - (4 * record + slot) for a leaf slot.
+template <bool kWide>
 __device__ __forceinline__ void trav_pop(Trav& tr, const DevScene& s, const int* sn, const float* st) {
   for (;;) {
     const int bottom = tr.level ? tr.blas_sp0 : 0;
@@ -81,7 +108,16 @@ __device__ __forceinline__ void trav_pop(Trav& tr, const DevScene& s, const int*
       --tr.sp;
       if (st[tr.sp] <= tr.t) {
         const int c = sn[tr.sp];
-        trav_enter(tr, c, load_node(s.nodes, tr.base + c));
+        if (!kWide) {
+          trav_enter(tr, c, load_node(s.nodes, tr.base + c));
+        } else if (c >= 0) {
+          tr.cur = c;
+          tr.mode = kTravNode;
+        } else {
+          const int k = -1 - c, sl = k & 3;
+          const int* rec = reinterpret_cast<const int*>(node4_at(s, k >> 2) + 6);
+          trav_enter_leaf(tr, __ldg(rec + sl), (__ldg(rec + 4) >> (8 * sl)) & 0xff);
+        }
         return;
       }
     }
@@ -99,7 +135,10 @@ __device__ __forceinline__ void trav_pop(Trav& tr, const DevScene& s, const int*
   }
 }
 
-template <bool kCount>
+// kWalk: which walk and whether it counts its visits
+enum : int { kWalkBinary = 0, kWalkCount = 1, kWalkWide = 2 };
+
+template <int kWalk>
 __device__ __forceinline__ void trav_init(Trav& tr, const DevScene& s, const Ray& ray, float tmax, TraceCounters* cnt) {
   tr.wr = ray;
   tr.winv = inv_dir(ray.d);
@@ -113,18 +152,92 @@ __device__ __forceinline__ void trav_init(Trav& tr, const DevScene& s, const Ray
   tr.ii = tr.ii_end = 0;
   tr.ti = tr.ti_end = 0;
   const NodeRec root = load_node(s.nodes, 0);
-  if (kCount) cnt->nodes++;
+  if (kWalk == kWalkCount) cnt->nodes++;
   float te;
-  if (box_hit_t(root.bmin, root.bmax, tr.wr, tr.winv, tr.t, &te)) trav_enter(tr, 0, root);
-  else tr.mode = kTravDone;
+  if (!box_hit_t(root.bmin, root.bmax, tr.wr, tr.winv, tr.t, &te)) {
+    tr.mode = kTravDone;
+  } else if (kWalk != kWalkWide || root.leaf) {
+    trav_enter(tr, 0, root);
+  } else {
+    tr.cur = 0;  // the TLAS root's record
+    tr.mode = kTravNode;
+  }
+}
+
+__device__ __forceinline__ float sel4(float a, float b, float c, float d, int i) {
+  return (i & 2) ? ((i & 1) ? d : c) : ((i & 1) ? b : a);
+}
+__device__ __forceinline__ int sel4(int a, int b, int c, int d, int i) {
+  return (i & 2) ? ((i & 1) ? d : c) : ((i & 1) ? b : a);
+}
+
+// one wide step: the four slot boxes of record tr.cur; returns false on stack overflow
+__device__ __forceinline__ bool trav_node4(Trav& tr, const DevScene& s, int* sn, float* st) {
+  const Ray& r = tr.level ? tr.orr : tr.wr;
+  const V3 inv = tr.level ? tr.oinv : tr.winv;
+  const float4* q = node4_at(s, tr.cur);
+  const float4 lx = __ldg(q), ly = __ldg(q + 1), lz = __ldg(q + 2);
+  const float4 hx = __ldg(q + 3), hy = __ldg(q + 4), hz = __ldg(q + 5);
+  const int4 ref = __ldg(reinterpret_cast<const int4*>(q + 6));
+  const int4 meta = __ldg(reinterpret_cast<const int4*>(q + 7));
+  float e0, e1, e2, e3;
+  const bool h0 = box_hit_t(mk(lx.x, ly.x, lz.x), mk(hx.x, hy.x, hz.x), r, inv, tr.t, &e0);
+  const bool h1 = box_hit_t(mk(lx.y, ly.y, lz.y), mk(hx.y, hy.y, hz.y), r, inv, tr.t, &e1);
+  const bool h2 = box_hit_t(mk(lx.z, ly.z, lz.z), mk(hx.z, hy.z, hz.z), r, inv, tr.t, &e2);
+  const bool h3 = box_hit_t(mk(lx.w, ly.w, lz.w), mk(hx.w, hy.w, hz.w), r, inv, tr.t, &e3);
+  const int hm = int(h0) | (int(h1) << 1) | (int(h2) << 2) | (int(h3) << 3);
+  if (!hm) {
+    trav_pop<true>(tr, s, sn, st);
+    return true;
+  }
+  // the binary walk's order: the near child's slots, then the far child's, each pair ordered by
+  // that child's own split axis (BVH.fs near-child rule at both levels)
+  const int m = meta.y;
+  const bool lf = comp(r.d, (m >> 4) & 3) > 0.f;
+  const bool fa = comp(r.d, lf ? ((m >> 6) & 3) : ((m >> 8) & 3)) > 0.f;
+  const bool fb = comp(r.d, lf ? ((m >> 8) & 3) : ((m >> 6) & 3)) > 0.f;
+  const int pa = lf ? 0 : 2, pb = 2 - pa;
+  int v[4];
+  v[0] = pa + (fa ? 0 : 1);
+  v[1] = pa + (fa ? 1 : 0);
+  v[2] = pb + (fb ? 0 : 1);
+  v[3] = pb + (fb ? 1 : 0);
+  int first = 3;
+#pragma unroll
+  for (int k = 2; k >= 0; --k)
+    if ((hm >> v[k]) & 1) first = k;
+  const int extra = __popc(hm) - 1;
+  if (tr.sp + extra > kStackSize) return false;
+  // stack the later hits so that they pop in visit order
+#pragma unroll
+  for (int k = 3; k >= 1; --k) {
+    const int sl = v[k];
+    if (k > first && ((hm >> sl) & 1)) {
+      sn[tr.sp] = ((m >> sl) & 1) ? -1 - (4 * tr.cur + sl) : sel4(ref.x, ref.y, ref.z, ref.w, sl);
+      st[tr.sp] = sel4(e0, e1, e2, e3, sl);
+      ++tr.sp;
+    }
+  }
+  const int sl = v[first];
+  const int rf = sel4(ref.x, ref.y, ref.z, ref.w, sl);
+  if ((m >> sl) & 1) trav_enter_leaf(tr, rf, (meta.x >> (8 * sl)) & 0xff);
+  else tr.cur = rf;
+  return true;
 }
 
 // one step (a node pair, one instance, and one triangle (kFine) or the rest of a leaf's
 // triangles); returns true once the walk is finished (tr.found / tr.hit hold the answer).
 // kFine suits lanes that are refilled with new rays; a single-ray walk runs fewer, coarser steps.
-template <bool kAny, bool kWT, bool kCount, bool kFine = true>
+template <bool kAny, bool kWT, int kWalk, bool kFine = true>
 __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, float* st, TraceCounters* cnt) {
-  if (tr.mode == kTravNode) {
+  constexpr bool kCount = kWalk == kWalkCount, kWide = kWalk == kWalkWide;
+  if (kWide && tr.mode == kTravNode) {
+    if (!trav_node4(tr, s, sn, st)) {
+      flag_error(s, BN_DEVERR_STACK_OVERFLOW);
+      tr.mode = kTravDone;
+      return true;
+    }
+  } else if (tr.mode == kTravNode) {
     const Ray& r = tr.level ? tr.orr : tr.wr;
     const V3 inv = tr.level ? tr.oinv : tr.winv;
     const int li = tr.cur + 1, ri = tr.n.link;
@@ -148,7 +261,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     } else if (hb) {
       trav_enter(tr, ri, b);
     } else {
-      trav_pop(tr, s, sn, st);
+      trav_pop<kWide>(tr, s, sn, st);
     }
   } else if (tr.mode == kTravTri) {
     // one triangle of a BLAS leaf: its AABB pre-test (Mesh.fs:204,231), then the triangle test
@@ -176,7 +289,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     }
     if (kFine) break;
     }
-    if (tr.ti >= tr.ti_end) trav_pop(tr, s, sn, st);
+    if (tr.ti >= tr.ti_end) trav_pop<kWide>(tr, s, sn, st);
   } else if (tr.mode == kTravInst) {
     // one instance of a TLAS leaf (PrimitiveInstance.Intersect, Primitive.fs:111-129)
     bool entered = false;
@@ -215,38 +328,43 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
           tr.tri_base = __ldg(&I->tri_base);
           tr.inst = k;
           tr.blas_sp0 = tr.sp;
-          trav_enter(tr, 0, root);
+          if (!kWide || root.leaf) {
+            trav_enter(tr, 0, root);
+          } else {
+            tr.cur = __ldg(&I->node4_root);
+            tr.mode = kTravNode;
+          }
           entered = true;
         }
       }
     }
     }
-    if (!entered && tr.ii >= tr.ii_end) trav_pop(tr, s, sn, st);
+    if (!entered && tr.ii >= tr.ii_end) trav_pop<kWide>(tr, s, sn, st);
   }
   return tr.mode == kTravDone;
 }
 
-template <bool kAny, bool kWT, bool kCount>
+template <bool kAny, bool kWT, int kWalk>
 __device__ __forceinline__ bool trace_walk(const DevScene& s, const Ray& ray, float tmax, HitRec* hit, TraceCounters* cnt) {
   int sn[kStackSize];
   float st[kStackSize];
   Trav tr;
-  trav_init<kCount>(tr, s, ray, tmax, cnt);
-  while (!trav_step<kAny, kWT, kCount, false>(tr, s, sn, st, cnt)) {
+  trav_init<kWalk>(tr, s, ray, tmax, cnt);
+  while (!trav_step<kAny, kWT, kWalk, false>(tr, s, sn, st, cnt)) {
   }
   if (!kAny) *hit = tr.hit;
   return tr.found;
 }
 
-template <bool kWT, bool kCount>
+template <bool kWT, int kWalk>
 __device__ __forceinline__ bool trace_closest(const DevScene& s, const Ray& ray, float tmax, HitRec* hit, TraceCounters* cnt) {
-  return trace_walk<false, kWT, kCount>(s, ray, tmax, hit, cnt);
+  return trace_walk<false, kWT, kWalk>(s, ray, tmax, hit, cnt);
 }
 
-template <bool kWT, bool kCount>
+template <bool kWT, int kWalk>
 __device__ __forceinline__ bool trace_any(const DevScene& s, const Ray& ray, float tmax, TraceCounters* cnt) {
   HitRec h;
-  return trace_walk<true, kWT, kCount>(s, ray, tmax, &h, cnt);
+  return trace_walk<true, kWT, kWalk>(s, ray, tmax, &h, cnt);
 }
 
 }  // namespace bn

@@ -4,6 +4,17 @@
 //             n0 = (min.x, min.y, min.z, max.x), n1 = (max.y, max.z, int right|offset,
 //             int bytes [is_leaf, split_axis, count, mask]).  TLAS first (root 0), then every
 //             mesh's BLAS at DevInstance::node_base.  Loaded as two 16-byte vector loads.
+//             The binary walk reads them when it counts visits (the reference's own work).
+//  nodes4     8 x float4 (128 B, one cache line) per interior node that the wide walk enters:
+//             the two binary levels below it in one record.  Slots 0-1 hold the left child's
+//             children (or the left child itself, slot 1 unused, when it is a leaf), slots 2-3
+//             the right child's.  (lo.x[4], lo.y[4], lo.z[4], hi.x[4], hi.y[4], hi.z[4]) slot
+//             boxes, int4 ref (node4 index of an interior slot, first item of a leaf slot),
+//             int4 meta (x: leaf item count, 8 bits per slot; y: leaf mask bits 0-3, split axis
+//             of the node << 4, of its left child << 6, of its right child << 8).  Unused slots
+//             have NaN boxes, which no ray enters.  TLAS records first (root at 0 when the TLAS
+//             root is interior), then every BLAS at DevInstance::node4_root.  Built when the
+//             scene is walked wide (DevScene::wide).
 //  tris       3 x float4 per triangle in BLAS-permuted order, all meshes back to back:
 //             (p0, material slot or -1), (p1, original index), (p2, 0).  48 bytes = the 12-byte
 //             index + 36 bytes of vertices the reference gathers per tested triangle.
@@ -35,7 +46,7 @@ struct alignas(16) DevInstance {
   int material;     // -1 = no material (a light only; the path ends there)
   int light;        // -1 = not emissive
   int light_entry_base;  // alias-triangles: entry index of triangle 0 of this instance, -1 if none
-  int mesh;         // mesh id (debug/statistics)
+  int node4_root;   // nodes4 record of the BLAS root; -1: binary scene, leaf root or sphere
 };
 static_assert(sizeof(DevInstance) == 160, "DevInstance layout");
 
@@ -76,6 +87,7 @@ struct DevView {
 
 struct DevScene {
   const float4* __restrict__ nodes;
+  const float4* __restrict__ nodes4;
   const float4* __restrict__ tris;
   const DevInstance* __restrict__ inst;
   const DevMaterial* __restrict__ mats;
@@ -86,6 +98,8 @@ struct DevScene {
   int n_inst;
   int n_tlas_nodes;
   int n_nodes;
+  int n_nodes4;
+  int wide;                               // walked through nodes4 (kWalkWide kernels)
   int n_tris;
   int n_light_inst;
   int n_tri_lights;

@@ -13,6 +13,7 @@
 // Gradients: lanes holding the same material slot are grouped (__match_any_sync), their FP32
 // values summed by shuffles, and one FP64 atomicAdd per group and parameter lands in HBM.
 #include "adjoint.hpp"
+#include "launch.hpp"
 #include "dev_shading.cuh"
 
 namespace bn {
@@ -108,7 +109,7 @@ __device__ __forceinline__ void grad_add(double* grad, int slot, const float g[k
 }
 
 // Li with value/sampling parameters; kGrad replays the path with its known total radiance
-template <bool kGrad>
+template <bool kGrad, int kWalk>
 __device__ V3 li_adj(const AdjParams& p, Ray ray, IndepSampler& smp, V3 L_total, V3 delta) {
   const DevScene& s = p.scene;
   V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f), beta_s = mk(1.f, 1.f, 1.f);
@@ -118,7 +119,7 @@ __device__ V3 li_adj(const AdjParams& p, Ray ray, IndepSampler& smp, V3 L_total,
   TraceCounters tc;
   while (depth < p.max_depth) {
     HitRec h;
-    if (!trace_closest<false, false>(s, ray, CUDART_INF_F, &h, &tc)) break;
+    if (!trace_closest<false, kWalk>(s, ray, CUDART_INF_F, &h, &tc)) break;
     const Interaction it = make_interaction(s, ray, h);
     const DevInstance* I = s.inst + it.inst;
     const int light = __ldg(&I->light);
@@ -152,7 +153,7 @@ __device__ V3 li_adj(const AdjParams& p, Ray ray, IndepSampler& smp, V3 L_total,
       Ray sh;
       sh.o = it.p;
       sh.d = ls.wi;
-      if (!trace_any<false, false>(s, sh, __fsub_rn(dist, 1e-3f), &tc)) {
+      if (!trace_any<false, kWalk>(s, sh, __fsub_rn(dist, 1e-3f), &tc)) {
         const V3 wi = to_local(it.f, ls.wi);
         const BsdfEval bes = bsdf_eval(ms, wo, wi);
         const BsdfEval bev = slotted ? bsdf_eval(mv, wo, wi) : bes;
@@ -224,6 +225,7 @@ __device__ __forceinline__ Ray adj_camera(const AdjParams& p, int x, int y, int 
   return camera_ray(*p.view, x, y, upx, upy, ulx, uly);
 }
 
+template <int kWalk>
 __global__ void __launch_bounds__(128) k_adj_forward(AdjParams p) {
   const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= p.n_pixels * p.spp) return;
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(128) k_adj_forward(AdjParams p) {
   path_pixel(p, i, &x, &y, &sid);
   IndepSampler smp;
   const Ray ray = adj_camera(p, x, y, sid, &smp);
-  const V3 L = li_adj<false>(p, ray, smp, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f));
+  const V3 L = li_adj<false, kWalk>(p, ray, smp, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f));
   p.path_L[i] = make_float4(L.x, L.y, L.z, 0.f);
 }
 
@@ -271,6 +273,7 @@ __global__ void k_adj_loss(AdjParams p) {
   if (threadIdx.x == 0) atomicAdd(p.loss, red[0]);
 }
 
+template <int kWalk>
 __global__ void __launch_bounds__(128) k_adj_backward(AdjParams p) {
   const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= p.n_pixels * p.spp) return;
@@ -285,14 +288,16 @@ __global__ void __launch_bounds__(128) k_adj_backward(AdjParams p) {
   const float4 Lt = p.path_L[i];
   IndepSampler smp;
   const Ray ray = adj_camera(p, x, y, sid, &smp);
-  li_adj<true>(p, ray, smp, mk(Lt.x, Lt.y, Lt.z), delta);
+  li_adj<true, kWalk>(p, ray, smp, mk(Lt.x, Lt.y, Lt.z), delta);
 }
 
 }  // namespace
 
 cudaError_t launch_adj_forward(const AdjParams& p, cudaStream_t st) {
   const long long n = p.n_pixels * p.spp;
-  k_adj_forward<<<(n + 127) / 128, 128, 0, st>>>(p);
+  dispatch_walk<false>(p.scene, false, false, [&](auto, auto walk) {
+    k_adj_forward<decltype(walk)::value><<<(n + 127) / 128, 128, 0, st>>>(p);
+  });
   return cudaGetLastError();
 }
 cudaError_t launch_adj_image(const AdjParams& p, cudaStream_t st) {
@@ -305,7 +310,9 @@ cudaError_t launch_adj_loss(const AdjParams& p, cudaStream_t st) {
 }
 cudaError_t launch_adj_backward(const AdjParams& p, cudaStream_t st) {
   const long long n = p.n_pixels * p.spp;
-  k_adj_backward<<<(n + 127) / 128, 128, 0, st>>>(p);
+  dispatch_walk<false>(p.scene, false, false, [&](auto, auto walk) {
+    k_adj_backward<decltype(walk)::value><<<(n + 127) / 128, 128, 0, st>>>(p);
+  });
   return cudaGetLastError();
 }
 

@@ -19,8 +19,9 @@ __device__ __forceinline__ int find_view(const long long* __restrict__ offsets, 
   return v;
 }
 
-template <bool kWT, bool kCount>
+template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_pt_mega(DevScene s, MegaParams p) {
+  constexpr bool kCount = kWalk == kWalkCount;
   const long long item = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   PathCounters pc{};
   unsigned long long paths = 0;
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(128) k_pt_mega(DevScene s, MegaParams p) {
       const float upx = smp.next(), upy = smp.next();
       const float ulx = smp.next(), uly = smp.next();
       const Ray ray = camera_ray(v, x, y, upx, upy, ulx, uly);
-      const V3 L = li_path<kWT, false, kCount>(s, ray, smp, p.max_depth, p.rr_depth, &pc);
+      const V3 L = li_path<kWT, false, kWalk>(s, ray, smp, p.max_depth, p.rr_depth, &pc);
       acc = fma3(mk(inv_spp, inv_spp, inv_spp), L, acc);
       ++paths;
     }
@@ -94,13 +95,9 @@ cudaError_t launch_megakernel(const DevScene& s, const MegaParams& p, cudaStream
   if (p.n_items <= 0) return cudaSuccess;
   const int bs = 128;
   const long long grid = (p.n_items + bs - 1) / bs;
-  if (p.watertight) {
-    if (p.count) k_pt_mega<true, true><<<grid, bs, 0, st>>>(s, p);
-    else k_pt_mega<true, false><<<grid, bs, 0, st>>>(s, p);
-  } else {
-    if (p.count) k_pt_mega<false, true><<<grid, bs, 0, st>>>(s, p);
-    else k_pt_mega<false, false><<<grid, bs, 0, st>>>(s, p);
-  }
+  dispatch_walk<true>(s, p.watertight, p.count, [&](auto wt, auto walk) {
+    k_pt_mega<decltype(wt)::value, decltype(walk)::value><<<grid, bs, 0, st>>>(s, p);
+  });
   return cudaGetLastError();
 }
 

@@ -14,6 +14,7 @@
 // AliasTable as built, which samples uniformly (Util/AliasTable.fs:20) unless the caller asks for
 // the proportional table (BN_RENDER_FIXED_ALIAS).
 #include "dev_shading.cuh"
+#include "launch.hpp"
 #include "pssmlt.hpp"
 
 namespace bn {
@@ -140,7 +141,7 @@ __device__ __forceinline__ Ray mlt_camera(const DevView& v, Smp& smp, int* px, i
   return camera_ray(v, x, y, fx, fy, lx, ly);
 }
 
-template <bool kWT>
+template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_mlt_bootstrap(MltParams p) {
   const int id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= p.n_bootstrap) return;
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(128) k_mlt_bootstrap(MltParams p) {
   int x, y;
   const Ray ray = mlt_camera(*p.view, smp, &x, &y);
   PathCounters pc{};
-  const V3 L = li_path<kWT, true, false>(p.scene, ray, smp, p.max_depth, p.rr_depth, &pc);
+  const V3 L = li_path<kWT, true, kWalk>(p.scene, ray, smp, p.max_depth, p.rr_depth, &pc);
   p.weights[id] = luminance(L);
 }
 
@@ -179,7 +180,7 @@ __device__ __forceinline__ void warp_splat(float* film, Splat s) {
   }
 }
 
-template <bool kWT>
+template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
   const int chain = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = chain < p.n_chains;
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
     m.start_iteration();
     int px, py;
     Ray ray = mlt_camera(v, m, &px, &py);
-    V3 L = li_path<kWT, true, false>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
+    V3 L = li_path<kWT, true, kWalk>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
     float y = luminance(L);
     m.accept();
     m.inner = xxhash32_three(static_cast<uint32_t>(chain), static_cast<uint32_t>(bid), static_cast<uint32_t>(p.frame_id));
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
       m.start_iteration();
       int nx, ny;
       ray = mlt_camera(v, m, &nx, &ny);
-      const V3 Ln = li_path<kWT, true, false>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
+      const V3 Ln = li_path<kWT, true, kWalk>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
       const float yn = luminance(Ln);
       const float ratio = __fdiv_rn(yn, y);
       const float acc = ratio != ratio ? ratio : fminf(1.f, ratio);  // MathF.Min propagates NaN
@@ -265,15 +266,17 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
 
 cudaError_t launch_mlt_bootstrap(const MltParams& p, cudaStream_t st) {
   const int grid = (p.n_bootstrap + 127) / 128;
-  if (p.watertight) k_mlt_bootstrap<true><<<grid, 128, 0, st>>>(p);
-  else k_mlt_bootstrap<false><<<grid, 128, 0, st>>>(p);
+  dispatch_walk<false>(p.scene, p.watertight, false, [&](auto wt, auto walk) {
+    k_mlt_bootstrap<decltype(wt)::value, decltype(walk)::value><<<grid, 128, 0, st>>>(p);
+  });
   return cudaGetLastError();
 }
 
 cudaError_t launch_mlt_chains(const MltParams& p, cudaStream_t st) {
   const int grid = (p.n_chains + 127) / 128;
-  if (p.watertight) k_mlt_chains<true><<<grid, 128, 0, st>>>(p);
-  else k_mlt_chains<false><<<grid, 128, 0, st>>>(p);
+  dispatch_walk<false>(p.scene, p.watertight, false, [&](auto wt, auto walk) {
+    k_mlt_chains<decltype(wt)::value, decltype(walk)::value><<<grid, 128, 0, st>>>(p);
+  });
   return cudaGetLastError();
 }
 

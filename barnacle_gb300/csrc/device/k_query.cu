@@ -25,9 +25,10 @@ __device__ __forceinline__ void warp_add_counters(DevCounters* c, unsigned long 
   }
 }
 
-template <bool kAny, bool kWT, bool kCount>
+template <bool kAny, bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_trace(DevScene s, const bn_ray* __restrict__ rays, bn_hit* __restrict__ hits,
                                                long long n, DevCounters* counters) {
+  constexpr bool kCount = kWalk == kWalkCount;
   const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   TraceCounters tc{0, 0, 0};
   unsigned long long nr = 0;
@@ -39,13 +40,13 @@ __global__ void __launch_bounds__(128) k_trace(DevScene s, const bn_ray* __restr
     bn_hit out{};
     nr = 1;
     if (kAny) {
-      const bool h = trace_any<kWT, kCount>(s, ray, r.t_max, &tc);
+      const bool h = trace_any<kWT, kWalk>(s, ray, r.t_max, &tc);
       out.instance = h ? 0 : -1;
       out.t = r.t_max;
       out.primitive = -1;
     } else {
       HitRec h;
-      if (trace_closest<kWT, kCount>(s, ray, r.t_max, &h, &tc)) {
+      if (trace_closest<kWT, kWalk>(s, ray, r.t_max, &h, &tc)) {
         const Interaction it = make_interaction(s, ray, h);
         out.t = h.t; out.u = it.u; out.v = it.v;
         out.instance = h.inst; out.primitive = h.tri;
@@ -67,11 +68,9 @@ cudaError_t launch_trace_t(const DevScene& s, const bn_ray* rays, bn_hit* hits, 
                            DevCounters* counters, cudaStream_t st) {
   const int bs = 128;
   const long long grid = (n + bs - 1) / bs;
-  const bool wt = flags & BN_TRACE_WATERTIGHT, cnt = flags & BN_TRACE_COUNT;
-  if (wt && cnt) k_trace<kAny, true, true><<<grid, bs, 0, st>>>(s, rays, hits, n, counters);
-  else if (wt) k_trace<kAny, true, false><<<grid, bs, 0, st>>>(s, rays, hits, n, counters);
-  else if (cnt) k_trace<kAny, false, true><<<grid, bs, 0, st>>>(s, rays, hits, n, counters);
-  else k_trace<kAny, false, false><<<grid, bs, 0, st>>>(s, rays, hits, n, counters);
+  dispatch_walk<true>(s, flags & BN_TRACE_WATERTIGHT, flags & BN_TRACE_COUNT, [&](auto wt, auto walk) {
+    k_trace<kAny, decltype(wt)::value, decltype(walk)::value><<<grid, bs, 0, st>>>(s, rays, hits, n, counters);
+  });
   return cudaGetLastError();
 }
 

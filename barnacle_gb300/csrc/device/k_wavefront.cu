@@ -114,7 +114,7 @@ __device__ __forceinline__ int fetch_next(int* counter, bool need) {
   return need ? base + __popc(m & ((1u << lane) - 1u)) : -1;
 }
 
-template <bool kWT>
+template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
@@ -134,11 +134,11 @@ __global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ 
       Ray ray;
       ray.o = mk(o.x, o.y, o.z);
       ray.d = mk(d.x, d.y, d.z);
-      trav_init<false>(tr, s, ray, CUDART_INF_F, &tc);
+      trav_init<kWalk>(tr, s, ray, CUDART_INF_F, &tc);
       need = false;
     }
     // a walk can end at init (root box missed)
-    if (tr.mode != kTravDone && !trav_step<false, kWT, false>(tr, s, sn, st, &tc)) continue;
+    if (tr.mode != kTravDone && !trav_step<false, kWT, kWalk>(tr, s, sn, st, &tc)) continue;
     need = true;
     int bin = kBinMiss;
     if (tr.found) {
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
   }
 }
 
-template <bool kWT>
+template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
@@ -298,10 +298,10 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ 
       Ray ray;
       ray.o = mk(o.x, o.y, o.z);
       ray.d = mk(d.x, d.y, d.z);
-      trav_init<false>(tr, p.scene, ray, o.w, &tc);
+      trav_init<kWalk>(tr, p.scene, ray, o.w, &tc);
       need = false;
     }
-    if (tr.mode != kTravDone && !trav_step<true, kWT, false>(tr, p.scene, sn, st, &tc))
+    if (tr.mode != kTravDone && !trav_step<true, kWT, kWalk>(tr, p.scene, sn, st, &tc))
       continue;
     need = true;
     if (!tr.found) {
@@ -360,14 +360,23 @@ int resident_grid(K kernel, int block) {
 
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st) {
   k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
+  auto go = [&](auto wt, auto walk) {
+    constexpr bool kWT = decltype(wt)::value;
+    constexpr int kWalk = decltype(walk)::value;
+    k_wf_extend<kWT, kWalk><<<l.grid_extend, 128, 0, st>>>(dparams);
+    k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
+    k_wf_shadow<kWT, kWalk><<<l.grid_shadow, 128, 0, st>>>(dparams);
+  };
+  using WT = std::integral_constant<bool, true>;
+  using MT = std::integral_constant<bool, false>;
+  using Bin = std::integral_constant<int, kWalkBinary>;
+  using Wide = std::integral_constant<int, kWalkWide>;
   if (l.watertight) {
-    k_wf_extend<true><<<l.grid_extend, 128, 0, st>>>(dparams);
-    k_wf_shade<true><<<l.grid_shade, 128, 0, st>>>(dparams);
-    k_wf_shadow<true><<<l.grid_shadow, 128, 0, st>>>(dparams);
+    if (l.wide) go(WT{}, Wide{});
+    else go(WT{}, Bin{});
   } else {
-    k_wf_extend<false><<<l.grid_extend, 128, 0, st>>>(dparams);
-    k_wf_shade<false><<<l.grid_shade, 128, 0, st>>>(dparams);
-    k_wf_shadow<false><<<l.grid_shadow, 128, 0, st>>>(dparams);
+    if (l.wide) go(MT{}, Wide{});
+    else go(MT{}, Bin{});
   }
   k_wf_control<<<1, 1, 0, st>>>(dparams, use_graph ? 1 : 0);
   return cudaGetLastError();
@@ -378,9 +387,10 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-WfLaunch wf_launch_shape(bool watertight, int blocks_per_sm_cap) {
+WfLaunch wf_launch_shape(bool watertight, bool wide, int blocks_per_sm_cap) {
   WfLaunch l{};
   l.watertight = watertight;
+  l.wide = wide;
   auto cap = [&](int g) {
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -388,14 +398,23 @@ WfLaunch wf_launch_shape(bool watertight, int blocks_per_sm_cap) {
     return blocks_per_sm_cap > 0 ? std::min(g, sms * blocks_per_sm_cap) : g;
   };
   l.grid_regen = cap(resident_grid(k_wf_regen, 256));
+  auto shape = [&](auto wt, auto walk) {
+    constexpr bool kWT = decltype(wt)::value;
+    constexpr int kWalk = decltype(walk)::value;
+    l.grid_extend = cap(resident_grid(k_wf_extend<kWT, kWalk>, 128));
+    l.grid_shade = cap(resident_grid(k_wf_shade<kWT>, 128));
+    l.grid_shadow = cap(resident_grid(k_wf_shadow<kWT, kWalk>, 128));
+  };
+  using WT = std::integral_constant<bool, true>;
+  using MT = std::integral_constant<bool, false>;
+  using Bin = std::integral_constant<int, kWalkBinary>;
+  using Wide = std::integral_constant<int, kWalkWide>;
   if (watertight) {
-    l.grid_extend = cap(resident_grid(k_wf_extend<true>, 128));
-    l.grid_shade = cap(resident_grid(k_wf_shade<true>, 128));
-    l.grid_shadow = cap(resident_grid(k_wf_shadow<true>, 128));
+    if (wide) shape(WT{}, Wide{});
+    else shape(WT{}, Bin{});
   } else {
-    l.grid_extend = cap(resident_grid(k_wf_extend<false>, 128));
-    l.grid_shade = cap(resident_grid(k_wf_shade<false>, 128));
-    l.grid_shadow = cap(resident_grid(k_wf_shadow<false>, 128));
+    if (wide) shape(MT{}, Wide{});
+    else shape(MT{}, Bin{});
   }
   return l;
 }

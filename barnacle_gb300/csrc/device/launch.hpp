@@ -2,10 +2,37 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "../../../include/barnacle_gpu.h"
 #include "dev_types.cuh"
 
 namespace bn {
+
+// Compile-time walk and triangle test of a launch: f(std::integral_constant<bool, watertight>,
+// std::integral_constant<int, walk>) with walk one of kWalkBinary / kWalkCount / kWalkWide
+// (dev_traverse.cuh).  A counting launch walks the binary tree; otherwise the scene's choice.
+template <bool kWithCount, class F>
+void dispatch_walk(const DevScene& s, bool watertight, bool count, F&& f) {
+  using WT = std::integral_constant<bool, true>;
+  using MT = std::integral_constant<bool, false>;
+  using Bin = std::integral_constant<int, 0>;
+  using Cnt = std::integral_constant<int, 1>;
+  using Wide = std::integral_constant<int, 2>;
+  const int walk = (kWithCount && count) ? 1 : (s.wide ? 2 : 0);
+  if (walk == 1) {
+    if constexpr (kWithCount) {
+      if (watertight) f(WT{}, Cnt{});
+      else f(MT{}, Cnt{});
+    }
+  } else if (walk == 2) {
+    if (watertight) f(WT{}, Wide{});
+    else f(MT{}, Wide{});
+  } else {
+    if (watertight) f(WT{}, Bin{});
+    else f(MT{}, Bin{});
+  }
+}
 
 // per-launch counters written by kernels that count (BN_TRACE_COUNT, stats renders)
 struct DevCounters {

@@ -52,9 +52,10 @@ struct WfParams {
 struct WfLaunch {
   int grid_regen, grid_extend, grid_shade, grid_shadow;
   bool watertight;
+  bool wide;                    // the scene's wide records (kWalkWide kernels)
 };
 
-WfLaunch wf_launch_shape(bool watertight, int blocks_per_sm_cap);
+WfLaunch wf_launch_shape(bool watertight, bool wide, int blocks_per_sm_cap);
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
 cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st);
 

@@ -162,6 +162,7 @@ def run_extras(ctx, args, torch, flush):
     out = {}
     # Cornell box: plain megakernel vs the CPU restatement (same workload, bounded CPU sample)
     c0 = Bundle.generate("cornell", 1)
+    c0.scene.contents.bvh_width = args.bvh_width
     ctx.upload(c0)
     r0 = c0.render
     r0.mode = capi.BN_MODE_MEGAKERNEL
@@ -266,6 +267,8 @@ def main():
                     help="skip the Cornell-box CPU ratio, PSSMLT and adjoint/forward measurements")
     ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0 = autotuned)")
     ap.add_argument("--cap", type=int, default=0, help="wavefront blocks per SM cap (0 = autotuned)")
+    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4],
+                    help="BVH walk: 0 = auto (wide records for BVHs of 64+ nodes), 2 = binary, 4 = wide")
     ap.add_argument("--no-graph", action="store_true",
                     help="wavefront bounce loop driven from the host (ncu cannot profile kernels inside a "
                          "graph with a conditional node)")
@@ -281,6 +284,7 @@ def main():
     dev = local if world > 1 else 0
     ctx = Context(dev)
     b = Bundle.generate(WORKLOAD, 1)
+    b.scene.contents.bvh_width = args.bvh_width
     ctx.upload(b)
     views = b.views
     r = b.render
@@ -381,7 +385,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
             "config": {"workload": f"{WORKLOAD}: 1024 instances of 4 displaced icospheres (20k/82k/200k/328k tris) "
                                    "+ 64 emissive triangles, 16 views 256x240..1920x1080, depth 12, rr 3",
-                       "mode": args.mode, "spp_per_step": r.spp, "pixels_per_step": pixels,
+                       "mode": args.mode, "bvh_width": {0: "auto", 2: "binary", 4: "wide"}[args.bvh_width], "spp_per_step": r.spp, "pixels_per_step": pixels,
                        "rays_per_step": int(rays_per_step),
                        "per_ray": {"nodes": st.nodes_visited / max(1, st.rays), "triangles": st.tris_tested / max(1, st.rays),
                                    "instances": st.instances_visited / max(1, st.rays)},

@@ -57,6 +57,11 @@ enum bn_light_sampler_type {
   BN_LIGHTS_UNIFORM = 0,        /* Extensions/LightSampler/Uniform.fs: uniform over emissive instances */
   BN_LIGHTS_ALIAS_TRIANGLES = 1 /* new plugin: Vose alias table over all emissive triangles, by power  */
 };
+/* How the device walks the scene's BVHs.  Both walks return identical hits (same visit order and
+ * box decisions as Aggregate/BVH.fs); they differ in speed only.  AUTO takes the 4-wide records
+ * for scenes of at least 1,024 BVH nodes, where halving the dependent node loads pays for the
+ * wider tests.  Visit counting (BN_TRACE_COUNT, BN_RENDER_COUNT) always walks the binary tree. */
+enum bn_bvh_width { BN_BVH_AUTO = 0, BN_BVH_BINARY = 2, BN_BVH_WIDE = 4 };
 
 /* MeshPrimitive(vertices, indices) (Extensions/Primitive/Mesh.fs:120) */
 typedef struct bn_mesh_desc {
@@ -117,6 +122,7 @@ typedef struct bn_scene_desc {
   const bn_material_desc* materials;   int32_t n_materials;
   const bn_light_desc* lights;         int32_t n_lights;
   int32_t light_sampler;               /* bn_light_sampler_type */
+  int32_t bvh_width;                   /* bn_bvh_width (0 = auto) */
 } bn_scene_desc;
 
 /* ---- ray queries (Extensions/Aggregate/BVH.fs:11-58) ----------------------------------- */

@@ -128,6 +128,64 @@ def test_watertight_and_moller_trumbore_agree_off_edges(ctx, loaded):
     np.testing.assert_allclose(wt["t"][both_hit], mt["t"][both_hit], rtol=1e-5)
 
 
+def plane_rays(bundle, n, rng):
+    """Rays that start exactly on BVH box planes (mesh vertices of identity-transformed
+    instances: every box bound is some vertex coordinate) with axis-aligned or random
+    directions, where a zero direction component meets a zero slab offset (0 * inf)."""
+    sc = bundle.scene.contents
+    pts = []
+    for i in range(sc.n_instances):
+        inst = sc.instances[i]
+        prim = sc.primitives[inst.primitive]
+        if prim.type != 0 or list(inst.object_to_world) != [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1]:
+            continue
+        m = sc.meshes[prim.mesh]
+        pts.append(np.ctypeslib.as_array(m.vertices, shape=(m.n_vertices * 3,)).reshape(-1, 3))
+    pts = np.concatenate(pts).astype(np.float32)
+    r = np.zeros(n, capi.RAY_DTYPE)
+    r["origin"] = pts[rng.integers(0, len(pts), n)]
+    # mixing coordinates of different vertices puts origins on several planes at once
+    mix = pts[rng.integers(0, len(pts), n)]
+    swap = rng.random((n, 3)) < 0.3
+    r["origin"] = np.where(swap, mix, r["origin"])
+    axes = np.eye(3, dtype=np.float32)[rng.integers(0, 3, n)] * rng.choice([-1, 1], size=(n, 1)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.sqrt((d ** 2).sum(1, dtype=np.float32))[:, None]
+    half = rng.random(n) < 0.5
+    r["direction"] = np.where(half[:, None], axes, d)
+    r["t_max"] = np.inf
+    return r
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_wide_walk_equals_binary_walk(ctx, loaded, name):
+    """The 4-wide record walk and the binary walk (taken when visits are counted) make the same
+    decisions: identical hit records, ties included, on scene rays and on rays that start on box
+    planes along axis directions."""
+    b, _ = loaded(ctx, name)
+    b.scene.contents.bvh_width = capi.BN_BVH_WIDE  # records for every BVH, small ones included
+    try:
+        ctx.upload(b)
+    finally:
+        b.scene.contents.bvh_width = capi.BN_BVH_AUTO
+    rng = np.random.default_rng(11)
+    rays = scene_rays(b, 40000, rng)
+    if name != "instances":
+        rays = np.concatenate([rays, plane_rays(b, 40000, rng)])
+    for flags in (0, capi.BN_TRACE_WATERTIGHT):
+        wide = ctx.trace(rays, flags)
+        binary = ctx.trace(rays, flags | capi.BN_TRACE_COUNT)
+        assert (binary["instance"] >= 0).mean() > 0.3
+        for f in ("instance", "primitive"):
+            assert np.array_equal(wide[f], binary[f]), f"{f}: {(wide[f] != binary[f]).sum()} differ"
+        for f in ("t", "u", "v"):
+            assert np.array_equal(wide[f].view(np.uint32), binary[f].view(np.uint32)), f
+    rays["t_max"] = rng.uniform(0.01, 2.0 if name != "instances" else 60.0, len(rays)).astype(np.float32)
+    wide = ctx.trace(rays, capi.BN_TRACE_ANY)
+    binary = ctx.trace(rays, capi.BN_TRACE_ANY | capi.BN_TRACE_COUNT)
+    assert np.array_equal(wide["instance"], binary["instance"])
+
+
 def test_trace_counters(ctx, loaded):
     b, o = loaded(ctx, "cornell-objects")
     rays = scene_rays(b, 5000, np.random.default_rng(5))
