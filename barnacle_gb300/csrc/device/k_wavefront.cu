@@ -101,7 +101,10 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
 
 // Persistent lanes with dynamic ray fetch: a lane whose ray finished claims the next queued ray
 // (one atomic per warp for all lanes that need one) and keeps stepping, so a warp never waits
-// out its slowest ray with idle lanes while work remains in the queue.
+// out its slowest ray with idle lanes while work remains in the queue.  Finished lanes wait until
+// at most refill_below lanes of the warp still walk and are then written out and refilled
+// together: the result stores, material lookups and ray loads are dependent-load chains, and
+// running them for one lane at a time would stall the whole warp on almost every step.
 __device__ __forceinline__ int fetch_next(int* counter, bool need) {
   const unsigned act = __activemask();
   const unsigned m = __ballot_sync(act, need);
@@ -119,51 +122,59 @@ __global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ 
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
   const int n = p.counters[kCntActive];
+  const int refill_below = p.refill_extend;
   int sn[kStackSize];
   float st[kStackSize];
   Trav tr;
   TraceCounters tc;
   int slot = -1;
-  bool need = true;
+  bool have = false, pending = false;
   for (;;) {
-    const int qi = fetch_next(&p.counters[kCntFetchRay], need);
-    if (need) {
-      if (qi >= n) break;
-      slot = p.q_active[qi];
-      const float4 o = p.ray_o[slot], d = p.ray_d[slot];
-      Ray ray;
-      ray.o = mk(o.x, o.y, o.z);
-      ray.d = mk(d.x, d.y, d.z);
-      trav_init<kWalk>(tr, s, ray, CUDART_INF_F, &tc);
-      need = false;
+    if (__popc(__ballot_sync(__activemask(), have)) <= refill_below) {
+      if (pending) {
+        pending = false;
+        int bin = kBinMiss;
+        if (tr.found) {
+          const HitRec& h = tr.hit;
+          p.hit_f[slot] = make_float4(h.t, h.u, h.v, 0.f);
+          p.hit_i[slot] = make_int2(h.inst, h.sphere_root ? h.sphere_root : h.tri);
+          const DevInstance* I = s.inst + h.inst;
+          int m = __ldg(&I->material);
+          if (m >= 0 && __ldg(&I->prim_type) == kPrimMesh) {
+            const int slot_m = __float_as_int(__ldg(&s.tris[3 * (__ldg(&I->tri_base) + h.tri)].w));
+            if (slot_m >= 0) m = slot_m;
+          }
+          bin = m < 0 ? kBinNoMaterial : s.mats[m].type;
+        } else {
+          p.hit_i[slot] = make_int2(-1, 0);
+        }
+        // material binning among the lanes finishing together: equal keys share one atomic
+        const unsigned act = __activemask();
+        const unsigned peers = __match_any_sync(act, bin);
+        const int leader = __ffs(peers) - 1;
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&p.counters[kCntBin0 + bin], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        p.q_bins[static_cast<long long>(bin) * p.pool + base + __popc(peers & ((1u << lane) - 1u))] = slot;
+      }
+      const int qi = fetch_next(&p.counters[kCntFetchRay], !have);
+      if (!have) {
+        if (qi >= n) break;
+        slot = p.q_active[qi];
+        const float4 o = p.ray_o[slot], d = p.ray_d[slot];
+        Ray ray;
+        ray.o = mk(o.x, o.y, o.z);
+        ray.d = mk(d.x, d.y, d.z);
+        trav_init<kWalk>(tr, s, ray, CUDART_INF_F, &tc);
+        have = true;
+      }
     }
     // a walk can end at init (root box missed)
-    if (tr.mode != kTravDone && !trav_step<false, kWT, kWalk>(tr, s, sn, st, &tc)) continue;
-    need = true;
-    int bin = kBinMiss;
-    if (tr.found) {
-      const HitRec& h = tr.hit;
-      p.hit_f[slot] = make_float4(h.t, h.u, h.v, 0.f);
-      p.hit_i[slot] = make_int2(h.inst, h.sphere_root ? h.sphere_root : h.tri);
-      const DevInstance* I = s.inst + h.inst;
-      int m = __ldg(&I->material);
-      if (m >= 0 && __ldg(&I->prim_type) == kPrimMesh) {
-        const int slot_m = __float_as_int(__ldg(&s.tris[3 * (__ldg(&I->tri_base) + h.tri)].w));
-        if (slot_m >= 0) m = slot_m;
-      }
-      bin = m < 0 ? kBinNoMaterial : s.mats[m].type;
-    } else {
-      p.hit_i[slot] = make_int2(-1, 0);
+    if (have && (tr.mode == kTravDone || trav_step<false, kWT, kWalk>(tr, s, sn, st, &tc))) {
+      have = false;
+      pending = true;
     }
-    // material binning among the lanes finishing together: equal keys share one atomic
-    const unsigned act = __activemask();
-    const unsigned peers = __match_any_sync(act, bin);
-    const int leader = __ffs(peers) - 1;
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&p.counters[kCntBin0 + bin], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    p.q_bins[static_cast<long long>(bin) * p.pool + base + __popc(peers & ((1u << lane) - 1u))] = slot;
   }
 }
 
@@ -282,37 +293,44 @@ template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
+  const int refill_below = p.refill_shadow;
   int sn[kStackSize];
   float st[kStackSize];
   Trav tr;
   TraceCounters tc;
   int rec = -1;
-  bool need = true;
+  bool have = false, pending = false;
   for (;;) {
-    const int qi = fetch_next(&p.counters[kCntFetchShadow], need);
-    if (need) {
-      if (qi >= n) break;
-      rec = qi;
-      const float4* r = p.shadow + 4LL * rec;
-      const float4 o = r[0], d = r[1];
-      Ray ray;
-      ray.o = mk(o.x, o.y, o.z);
-      ray.d = mk(d.x, d.y, d.z);
-      trav_init<kWalk>(tr, p.scene, ray, o.w, &tc);
-      need = false;
+    if (__popc(__ballot_sync(__activemask(), have)) <= refill_below) {
+      if (pending) {
+        pending = false;
+        if (!tr.found) {
+          const float4* r = p.shadow + 4LL * rec;
+          const int slot = __float_as_int(r[1].w);
+          const float4 a = r[2], b = r[3];
+          float4 L = p.L[slot];
+          L.x = fmaf(a.x, b.x, L.x);
+          L.y = fmaf(a.y, b.y, L.y);
+          L.z = fmaf(a.z, b.z, L.z);
+          p.L[slot] = L;
+        }
+      }
+      const int qi = fetch_next(&p.counters[kCntFetchShadow], !have);
+      if (!have) {
+        if (qi >= n) break;
+        rec = qi;
+        const float4* r = p.shadow + 4LL * rec;
+        const float4 o = r[0], d = r[1];
+        Ray ray;
+        ray.o = mk(o.x, o.y, o.z);
+        ray.d = mk(d.x, d.y, d.z);
+        trav_init<kWalk>(tr, p.scene, ray, o.w, &tc);
+        have = true;
+      }
     }
-    if (tr.mode != kTravDone && !trav_step<true, kWT, kWalk>(tr, p.scene, sn, st, &tc))
-      continue;
-    need = true;
-    if (!tr.found) {
-      const float4* r = p.shadow + 4LL * rec;
-      const int slot = __float_as_int(r[1].w);
-      const float4 a = r[2], b = r[3];
-      float4 L = p.L[slot];
-      L.x = fmaf(a.x, b.x, L.x);
-      L.y = fmaf(a.y, b.y, L.y);
-      L.z = fmaf(a.z, b.z, L.z);
-      p.L[slot] = L;
+    if (have && (tr.mode == kTravDone || trav_step<true, kWT, kWalk>(tr, p.scene, sn, st, &tc))) {
+      have = false;
+      pending = true;
     }
   }
 }

@@ -28,6 +28,8 @@ struct WfParams {
   int spp, max_depth, rr_depth, frame_id;
   int pool;                     // path slots
   int max_iters;                // watchdog
+  int refill_extend;            // extend lanes refill when at most this many of a warp still walk
+  int refill_shadow;            // the same for the shadow kernel
   long long total_paths;
   long long n_pixels;
   // per slot
