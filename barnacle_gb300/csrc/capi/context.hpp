@@ -45,6 +45,7 @@ struct bn_context {
   std::vector<bn::DevMaterial> host_mats;
   std::vector<int32_t> host_inst_light;  // per TLAS instance: light index
   int n_lights = 0;
+  float scene_lo[3] = {0.f, 0.f, 0.f}, scene_hi[3] = {0.f, 0.f, 0.f};  // TLAS root box
 
   // queries
   DevBuf q_in, q_out;

@@ -434,6 +434,10 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   s.light_sampler = d->light_sampler;
   s.n_mats = d->n_materials;
   s.error_word = ctx->error_word.as<unsigned int>();
+  for (int a = 0; a < 3; ++a) {
+    ctx->scene_lo[a] = tlas[0].bounds_min[a];
+    ctx->scene_hi[a] = tlas[0].bounds_max[a];
+  }
   ctx->inst_order.assign(order.begin(), order.end());
   ctx->host_mats = mats;
   ctx->host_inst_light = inst_light;

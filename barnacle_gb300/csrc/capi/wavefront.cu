@@ -1,6 +1,7 @@
 // Wavefront render orchestration: path-state buffers, the CUDA graph whose while-node runs the
 // whole bounce loop on the device, the host-driven fallback loop, and the launch autotuner.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -13,6 +14,7 @@ namespace {
 struct WfState {
   int pool = 0;
   DevBuf params, ray_o, ray_d, beta, L, meta, hit_f, hit_i, q_active, q_bins, shadow, counters, work_next, film_acc;
+  DevBuf slot_key, q_key, q_ray, sh_key, q_shadow, hist, off;
   // captured graph (one per launch shape)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -27,7 +29,7 @@ struct WfState {
 
   void release() {
     DevBuf* b[] = {&params, &ray_o, &ray_d, &beta, &L, &meta, &hit_f, &hit_i, &q_active, &q_bins, &shadow, &counters,
-                   &work_next, &film_acc};
+                   &work_next, &film_acc, &slot_key, &q_key, &q_ray, &sh_key, &q_shadow, &hist, &off};
     for (DevBuf* x : b) x->release();
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -65,6 +67,10 @@ cudaError_t ensure_pool(WfState* w, int pool) {
   if ((e = w->shadow.reserve(P * 4 * sizeof(float4))) != cudaSuccess) return e;
   if ((e = w->counters.reserve(bn::kCntSize * sizeof(int))) != cudaSuccess) return e;
   if ((e = w->work_next.reserve(sizeof(unsigned long long))) != cudaSuccess) return e;
+  for (DevBuf* b : {&w->slot_key, &w->q_key, &w->q_ray, &w->sh_key, &w->q_shadow})
+    if ((e = b->reserve(P * sizeof(int))) != cudaSuccess) return e;
+  if ((e = w->hist.reserve(bn::kSortBins * sizeof(unsigned))) != cudaSuccess) return e;
+  if ((e = w->off.reserve((bn::kSortBins + bn::kSortBins / 1024) * sizeof(unsigned))) != cudaSuccess) return e;
   w->pool = pool;
   return cudaSuccess;
 }
@@ -113,8 +119,12 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
     return ctx->cuda_fail(e, "wavefront film allocation");
   const bool wt = d->flags & BN_RENDER_WATERTIGHT;
   const bool wide = ctx->scene.wide != 0;
-  if (w->shape_cap != cap || w->shape.watertight != wt || w->shape.wide != wide) {
-    w->shape = bn::wf_launch_shape(wt, wide, cap);
+  // both queues sorted by ray key: on the 1,024-instance workload 111.5 M paths/s against 110.0
+  // (ray queue only) and 107.9 (neither)
+  const bool sort = true, sort_shadow = true;
+  if (w->shape_cap != cap || w->shape.watertight != wt || w->shape.wide != wide || w->shape.sort != sort ||
+      w->shape.sort_shadow != sort_shadow) {
+    w->shape = bn::wf_launch_shape(wt, wide, sort, sort_shadow, cap);
     w->shape_cap = cap;
     if (w->exec) {
       cudaGraphExecDestroy(w->exec);
@@ -145,6 +155,25 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.hit_f = w->hit_f.as<float4>();
   p.hit_i = w->hit_i.as<int2>();
   p.q_active = w->q_active.as<int>();
+  p.sort = sort ? 1 : 0;
+  p.sort_shadow = sort_shadow ? 1 : 0;
+  {
+    float lo[3], sc[3];
+    for (int a = 0; a < 3; ++a) {
+      const float ext = ctx->scene_hi[a] - ctx->scene_lo[a];
+      lo[a] = ctx->scene_lo[a];
+      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : 32.f) / ext : 0.f;
+    }
+    p.key_lo = make_float4(lo[0], lo[1], lo[2], 0.f);
+    p.key_scale = make_float4(sc[0], sc[1], sc[2], 0.f);
+  }
+  p.slot_key = w->slot_key.as<int>();
+  p.q_key = w->q_key.as<int>();
+  p.q_ray = sort ? w->q_ray.as<int>() : w->q_active.as<int>();
+  p.sh_key = w->sh_key.as<int>();
+  p.q_shadow = w->q_shadow.as<int>();
+  p.hist = w->hist.as<unsigned>();
+  p.off = w->off.as<unsigned>();
   p.q_bins = w->q_bins.as<int>();
   p.shadow = w->shadow.as<float4>();
   p.counters = w->counters.as<int>();
@@ -162,6 +191,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   cudaStream_t st = ctx->stream;
   cudaMemcpyAsync(w->params.ptr, &p, sizeof(p), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(w->counters.ptr, 0, bn::kCntSize * sizeof(int), st);
+  cudaMemsetAsync(w->hist.ptr, 0, bn::kSortBins * sizeof(unsigned), st);
   cudaMemsetAsync(w->work_next.ptr, 0, sizeof(unsigned long long), st);
   cudaMemsetAsync(w->meta.ptr, 0, static_cast<size_t>(pool) * sizeof(int4), st);
   cudaMemsetAsync(w->film_acc.ptr, 0, static_cast<size_t>(n_pixels) * 3 * sizeof(double), st);
@@ -173,7 +203,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
     for (int it = 0; it < p.max_iters + 1; ++it) {
       if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st)) != cudaSuccess)
         return ctx->cuda_fail(e, "wavefront iteration launch");
-      launches += 5;
+      launches += 5 + (sort ? 3 : 0) + (sort_shadow ? 3 : 0);
       int again = 0;
       cudaMemcpyAsync(&again, w->counters.as<int>() + bn::kCntAgain, sizeof(int), cudaMemcpyDeviceToHost, st);
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront iteration");
@@ -190,7 +220,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   float ms_loop = 0.f, ms_all = 0.f;
   cudaEventElapsedTime(&ms_loop, ctx->ev0, ctx->ev1);
   cudaEventElapsedTime(&ms_all, ctx->ev0, ctx->ev2);
-  if (use_graph) launches = 5 * counters[bn::kCntIter];
+  if (use_graph) launches = (5 + (sort ? 3 : 0) + (sort_shadow ? 3 : 0)) * counters[bn::kCntIter];
   ctx->stats.last_kernel_ms = ms_all;
   ctx->stats.last_dominant_ms = ms_loop;
   ctx->stats.last_launches = launches + 1;

@@ -1,13 +1,15 @@
 // The batched wavefront form of PathTracingIntegrator.Li (PathTracing.fs:14-81) over many views.
 //
-// A pool of P path slots lives in HBM (SoA).  One iteration of the bounce loop is five kernels:
+// A pool of P path slots lives in HBM (SoA).  One iteration of the bounce loop is:
 //   regen    every slot: retire a finished path into the FP64 film, refill free slots with new
 //            camera paths (warp-aggregated claims on a global path counter), and append the
-//            active slots to the ray queue (ballot + popc compaction)
+//            active slots to the ray queue (ballot + popc compaction) with their sort keys
+//   sort     counting sort of the ray queue by key (octant, origin cell): scan + scatter
 //   extend   closest hit for the ray queue; each hit is binned by the material type it shades
 //            with (__match_any_sync groups, one atomic per group) so shading runs type-sorted
 //   shade    emission with MIS, light sample + BSDF eval (a shadow-ray record), BSDF sample,
 //            Russian roulette; marks paths that end
+//   sort     the same counting sort of the shadow queue
 //   shadow   any hit for the shadow queue; unoccluded records add their NEE term to L
 //   control  one thread: decides whether another iteration is needed, resets the counters and
 //            sets the CUDA-graph while-condition (or a flag for host-driven loops); an iteration
@@ -40,6 +42,34 @@ __device__ __forceinline__ int find_view(const WfParams& p, long long id) {
   int v = 0;
   while (v + 1 < p.n_views && p.views[v + 1].path_offset <= id) ++v;
   return v;
+}
+
+// Sort key of a ray: direction octant over the Morton code of the origin's cell in a 32 x 8 x 32
+// grid over the scene bounds.  Rays next to each other in key order start in the same region in
+// the same octant, so a warp of them walks much the same nodes.
+__device__ __forceinline__ int ray_key(const WfParams& p, V3 o, V3 d) {
+  // fmaxf maps a NaN coordinate to cell 0
+  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), 31.f));
+  const unsigned y = static_cast<unsigned>(fminf(fmaxf((o.y - p.key_lo.y) * p.key_scale.y, 0.f), 7.f));
+  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), 31.f));
+  // interleave x4 z4 y2 x3 z3 y1 x2 z2 y0 x1 z1 x0 z0 (13 bits)
+  unsigned m = 0;
+  int b = 0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    m |= ((z >> k) & 1u) << b++;
+    m |= ((x >> k) & 1u) << b++;
+    if (k >= 2) m |= ((y >> (k - 2)) & 1u) << b++;
+  }
+  const unsigned oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  return static_cast<int>((oct << 13) | m);
+}
+
+// histogram of the keys of the lanes with pred; lanes with equal keys share one atomic.  Called
+// by whole warps.
+__device__ __forceinline__ void hist_add(unsigned* hist, int key, bool pred) {
+  const unsigned peers = __match_any_sync(0xffffffffu, pred ? key : -1);
+  if (pred && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(hist + key, static_cast<unsigned>(__popc(peers)));
 }
 
 __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ pp) {
@@ -85,6 +115,7 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
         const Ray ray = camera_ray(v, x, y, upx, upy, ulx, uly);
         p.ray_o[slot] = make_float4(ray.o.x, ray.o.y, ray.o.z, 0.f);
         p.ray_d[slot] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f);  // .w: pdf of the last BSDF sample
+        if (p.sort) p.slot_key[slot] = ray_key(p, ray.o, ray.d);
         p.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
         p.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
         const long long film_pix = v.pixel_offset + static_cast<long long>(v.height - y - 1) * v.width + x;
@@ -95,6 +126,11 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
     const bool active = valid && m.w == kStatusActive;
     const int qi = warp_append(&p.counters[kCntActive], active);
     if (active) p.q_active[qi] = slot;
+    if (p.sort) {
+      const int key = active ? p.slot_key[slot] : 0;
+      if (active) p.q_key[qi] = key;
+      hist_add(p.hist, key, active);
+    }
     if (valid) p.meta[slot] = m;
   }
 }
@@ -161,7 +197,7 @@ __global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ 
       const int qi = fetch_next(&p.counters[kCntFetchRay], !have);
       if (!have) {
         if (qi >= n) break;
-        slot = p.q_active[qi];
+        slot = p.q_ray[qi];
         const float4 o = p.ray_o[slot], d = p.ray_d[slot];
         Ray ray;
         ray.o = mk(o.x, o.y, o.z);
@@ -263,6 +299,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
               cont = true;
               p.ray_o[slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
               p.ray_d[slot] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
+              if (p.sort) p.slot_key[slot] = ray_key(p, it.p, nd);
               p.beta[slot] = make_float4(beta.x, beta.y, beta.z, 0.f);
               m.y = depth + 1;
             } else {
@@ -280,6 +317,11 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
     if (shadow) {
       float4* r = p.shadow + 4LL * si;
       r[0] = sh_o; r[1] = sh_d; r[2] = sh_a; r[3] = sh_b;
+    }
+    if (p.sort_shadow) {
+      const int key = shadow ? ray_key(p, mk(sh_o.x, sh_o.y, sh_o.z), mk(sh_d.x, sh_d.y, sh_d.z)) : 0;
+      if (shadow) p.sh_key[si] = key;
+      hist_add(p.hist, key, shadow);
     }
     const unsigned cm = __ballot_sync(0xffffffffu, cont), dm = __ballot_sync(0xffffffffu, done);
     if ((threadIdx.x & 31) == 0) {
@@ -318,7 +360,7 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ 
       const int qi = fetch_next(&p.counters[kCntFetchShadow], !have);
       if (!have) {
         if (qi >= n) break;
-        rec = qi;
+        rec = p.sort_shadow ? p.q_shadow[qi] : qi;
         const float4* r = p.shadow + 4LL * rec;
         const float4 o = r[0], d = r[1];
         Ray ray;
@@ -332,6 +374,80 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ 
       have = false;
       pending = true;
     }
+  }
+}
+
+// counting sort, steps 1-2: bucket offsets = exclusive scan of the counts, over kSortBins / 1024
+// tiles of 1024 bins (one block each): step 1 sums every tile, step 2 scans its tile on top of
+// the sums of the tiles before it and clears the counts for the next use
+constexpr int kScanTiles = kSortBins / 1024;
+
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned* total) {
+  __shared__ unsigned warp_sum[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned w = warp_sum[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_sum[lane] = w;
+  }
+  __syncthreads();
+  *total = warp_sum[31];
+  return x - v + (wid ? warp_sum[wid - 1] : 0u);
+}
+
+__global__ void __launch_bounds__(1024) k_wf_sort_tiles(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  unsigned total;
+  block_exclusive_scan(p.hist[blockIdx.x * 1024 + threadIdx.x], &total);
+  if (threadIdx.x == 0) p.off[kSortBins + blockIdx.x] = total;  // tile sums after the offsets
+}
+
+__global__ void __launch_bounds__(1024) k_wf_sort_scan(const WfParams* __restrict__ pp) {
+  const WfParams& p = *pp;
+  __shared__ unsigned tile_base;
+  if (threadIdx.x < 32) {
+    unsigned b = 0;
+    for (int t = threadIdx.x; t < static_cast<int>(blockIdx.x); t += 32) b += p.off[kSortBins + t];
+    for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
+    if (threadIdx.x == 0) tile_base = b;
+  }
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const unsigned c = p.hist[i];
+  unsigned total;
+  const unsigned x = block_exclusive_scan(c, &total);  // its barriers also publish tile_base
+  p.off[i] = tile_base + x;
+  p.hist[i] = 0u;
+}
+
+// counting sort, step 2: every queue entry to its bucket (order within a bucket is arbitrary;
+// per-path results do not depend on it)
+__global__ void __launch_bounds__(256) k_wf_sort_scatter(const WfParams* __restrict__ pp, int shadow_queue) {
+  const WfParams& p = *pp;
+  const int n = p.counters[shadow_queue ? kCntShadow : kCntActive];
+  const int* keys = shadow_queue ? p.sh_key : p.q_key;
+  int* out = shadow_queue ? p.q_shadow : p.q_ray;
+  const int stride = gridDim.x * blockDim.x;
+  const int nw = (n + 31) & ~31;
+  const int lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
+    const bool valid = i < n;
+    const int key = valid ? keys[i] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (valid && lane == leader) base = atomicAdd(p.off + key, static_cast<unsigned>(__popc(peers)));
+    base = __shfl_sync(peers, base, leader);
+    if (valid) out[base + __popc(peers & ((1u << lane) - 1u))] = shadow_queue ? i : p.q_active[i];
   }
 }
 
@@ -378,11 +494,19 @@ int resident_grid(K kernel, int block) {
 
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st) {
   k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
+  auto sort = [&](int shadow_queue) {
+    if (!l.sort || (shadow_queue && !l.sort_shadow)) return;
+    k_wf_sort_tiles<<<kScanTiles, 1024, 0, st>>>(dparams);
+    k_wf_sort_scan<<<kScanTiles, 1024, 0, st>>>(dparams);
+    k_wf_sort_scatter<<<l.grid_scatter, 256, 0, st>>>(dparams, shadow_queue);
+  };
   auto go = [&](auto wt, auto walk) {
     constexpr bool kWT = decltype(wt)::value;
     constexpr int kWalk = decltype(walk)::value;
+    sort(0);
     k_wf_extend<kWT, kWalk><<<l.grid_extend, 128, 0, st>>>(dparams);
     k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
+    sort(1);
     k_wf_shadow<kWT, kWalk><<<l.grid_shadow, 128, 0, st>>>(dparams);
   };
   using WT = std::integral_constant<bool, true>;
@@ -405,10 +529,12 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-WfLaunch wf_launch_shape(bool watertight, bool wide, int blocks_per_sm_cap) {
+WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, int blocks_per_sm_cap) {
   WfLaunch l{};
   l.watertight = watertight;
   l.wide = wide;
+  l.sort = sort;
+  l.sort_shadow = sort && sort_shadow;
   auto cap = [&](int g) {
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -416,6 +542,7 @@ WfLaunch wf_launch_shape(bool watertight, bool wide, int blocks_per_sm_cap) {
     return blocks_per_sm_cap > 0 ? std::min(g, sms * blocks_per_sm_cap) : g;
   };
   l.grid_regen = cap(resident_grid(k_wf_regen, 256));
+  l.grid_scatter = resident_grid(k_wf_sort_scatter, 256);
   auto shape = [&](auto wt, auto walk) {
     constexpr bool kWT = decltype(wt)::value;
     constexpr int kWalk = decltype(walk)::value;

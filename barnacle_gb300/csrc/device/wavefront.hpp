@@ -8,6 +8,9 @@
 namespace bn {
 
 constexpr int kNumBins = 6;  // 4 material types, miss, no material
+// ray-queue sort keys: direction octant (3 bits) over the Morton code (13 bits) of the origin's
+// cell in a 32 x 8 x 32 grid (x, y, z) over the scene bounds
+constexpr int kSortBits = 16, kSortBins = 1 << kSortBits;
 enum : int {
   kCntActive = 0,   // ray-queue length
   kCntShadow = 1,   // shadow-queue length
@@ -43,6 +46,16 @@ struct WfParams {
   // queues
   int* q_active;                // pool entries
   int* q_bins;                  // kNumBins x pool entries
+  // spatial sort of both ray queues (counting sort by key, when sort != 0)
+  int sort, sort_shadow;
+  float4 key_lo, key_scale;     // origin cell = (o - key_lo) * key_scale, in [0, 32) x [0, 8) x [0, 32)
+  int* slot_key;                // per slot: key of the ray the slot holds (written by shade)
+  int* q_key;                   // per ray-queue entry: its key
+  int* q_ray;                   // the ray queue in key order (read by extend)
+  int* sh_key;                  // per shadow record: its key
+  int* q_shadow;                // shadow-record indices in key order (read by shadow)
+  unsigned* hist;               // kSortBins counts; zero between uses (the scan clears it)
+  unsigned* off;                // kSortBins bucket offsets, then kSortBins / 1024 tile sums
   float4* shadow;               // 4 float4 per record: (o, tmax), (d, owner), a, b
   int* counters;                // kCntSize ints
   unsigned long long* work_next;
@@ -52,12 +65,13 @@ struct WfParams {
 };
 
 struct WfLaunch {
-  int grid_regen, grid_extend, grid_shade, grid_shadow;
+  int grid_regen, grid_extend, grid_shade, grid_shadow, grid_scatter;
   bool watertight;
   bool wide;                    // the scene's wide records (kWalkWide kernels)
+  bool sort, sort_shadow;       // ray / shadow queue sorted by ray key before extend / shadow
 };
 
-WfLaunch wf_launch_shape(bool watertight, bool wide, int blocks_per_sm_cap);
+WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, int blocks_per_sm_cap);
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
 cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st);
 
