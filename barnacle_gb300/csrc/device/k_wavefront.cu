@@ -154,7 +154,7 @@ __device__ __forceinline__ int fetch_next(int* counter, bool need) {
 }
 
 template <bool kWT, int kWalk>
-__global__ void __launch_bounds__(128) k_wf_extend(const WfParams* __restrict__ pp) {
+__global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
   const int n = p.counters[kCntActive];
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
 }
 
 template <bool kWT, int kWalk>
-__global__ void __launch_bounds__(128) k_wf_shadow(const WfParams* __restrict__ pp) {
+__global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
   const int refill_below = p.refill_shadow;
