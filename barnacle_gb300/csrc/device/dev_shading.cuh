@@ -387,7 +387,8 @@ struct PathCounters {
 // PSSMLTIntegrator.Li (PSSMLT.fs:172-245), which draws 7 samples per bounce in a fixed order.
 // Draw order per bounce: u_select, u_light.xy (NEE), u_lobe, u_bsdf.xy, then u_rr if depth >=
 // rr_depth (PathTracing) / always (PSSMLT).  Reciprocal estimates are exact reciprocals here.
-template <bool kWT, bool kFixed7, int kWalk, class Smp>
+// kOutline: one out-of-line walk for both queries (see trace_walk_outline).
+template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false>
 __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int max_depth, int rr_depth, PathCounters* pc) {
   constexpr bool kCount = kWalk == kWalkCount;
   V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
@@ -396,7 +397,7 @@ __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int 
   while (depth < max_depth) {
     HitRec h;
     if (kCount) pc->rays++;
-    if (!trace_closest<kWT, kWalk>(s, ray, CUDART_INF_F, &h, &pc->tc)) break;
+    if (!trace_closest<kWT, kWalk, kOutline>(s, ray, CUDART_INF_F, &h, &pc->tc)) break;
     const Interaction it = make_interaction(s, ray, h);
     const DevInstance* I = s.inst + it.inst;
     if (__ldg(&I->light) >= 0) {
@@ -423,7 +424,7 @@ __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int 
       sh.o = it.p;
       sh.d = ls.wi;
       if (kCount) pc->rays++;
-      if (!trace_any<kWT, kWalk>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
+      if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
         const BsdfEval be = bsdf_eval(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
         L = fma3(mul(beta, be.f), scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L), L);
       }

@@ -60,6 +60,7 @@ struct Trav {
   int ii, ii_end;    // instances of the TLAS leaf being processed
   int ti, ti_end;    // triangles of the BLAS leaf being processed
   bool found;
+  bool any;          // any-hit query (runtime choice, kAnyRuntime walks)
   HitRec hit;
 };
 
@@ -171,8 +172,10 @@ __device__ __forceinline__ int sel4(int a, int b, int c, int d, int i) {
   return (i & 2) ? ((i & 1) ? d : c) : ((i & 1) ? b : a);
 }
 
-// one wide step: the four slot boxes of record tr.cur; returns false on stack overflow
-__device__ __forceinline__ bool trav_node4(Trav& tr, const DevScene& s, int* sn, float* st) {
+// one wide step: the four slot boxes of record tr.cur; returns kStepPop when none is entered,
+// kStepOverflow when the stack is full
+enum : int { kStepOk = 0, kStepPop = 1, kStepOverflow = 2 };
+__device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, float* st) {
   const Ray& r = tr.level ? tr.orr : tr.wr;
   const V3 inv = tr.level ? tr.oinv : tr.winv;
   const float4* q = node4_at(s, tr.cur);
@@ -186,10 +189,7 @@ __device__ __forceinline__ bool trav_node4(Trav& tr, const DevScene& s, int* sn,
   const bool h2 = box_hit_t(mk(lx.z, ly.z, lz.z), mk(hx.z, hy.z, hz.z), r, inv, tr.t, &e2);
   const bool h3 = box_hit_t(mk(lx.w, ly.w, lz.w), mk(hx.w, hy.w, hz.w), r, inv, tr.t, &e3);
   const int hm = int(h0) | (int(h1) << 1) | (int(h2) << 2) | (int(h3) << 3);
-  if (!hm) {
-    trav_pop<true>(tr, s, sn, st);
-    return true;
-  }
+  if (!hm) return kStepPop;
   // the binary walk's order: the near child's slots, then the far child's, each pair ordered by
   // that child's own split axis (BVH.fs near-child rule at both levels)
   const int m = meta.y;
@@ -207,7 +207,7 @@ __device__ __forceinline__ bool trav_node4(Trav& tr, const DevScene& s, int* sn,
   for (int k = 2; k >= 0; --k)
     if ((hm >> v[k]) & 1) first = k;
   const int extra = __popc(hm) - 1;
-  if (tr.sp + extra > kStackSize) return false;
+  if (tr.sp + extra > kStackSize) return kStepOverflow;
   // stack the later hits so that they pop in visit order
 #pragma unroll
   for (int k = 3; k >= 1; --k) {
@@ -222,21 +222,28 @@ __device__ __forceinline__ bool trav_node4(Trav& tr, const DevScene& s, int* sn,
   const int rf = sel4(ref.x, ref.y, ref.z, ref.w, sl);
   if ((m >> sl) & 1) trav_enter_leaf(tr, rf, (meta.x >> (8 * sl)) & 0xff);
   else tr.cur = rf;
-  return true;
+  return kStepOk;
 }
 
 // one step (a node pair, one instance, and one triangle (kFine) or the rest of a leaf's
 // triangles); returns true once the walk is finished (tr.found / tr.hit hold the answer).
 // kFine suits lanes that are refilled with new rays; a single-ray walk runs fewer, coarser steps.
-template <bool kAny, bool kWT, int kWalk, bool kFine = true>
+// kAny: kClosest, kAnyHit, or kAnyRuntime (tr.any decides).  Every branch that exhausts its unit
+// asks for a pop, which runs once at the end of the step.
+enum : int { kClosest = 0, kAnyHit = 1, kAnyRuntime = 2 };
+template <int kAny, bool kWT, int kWalk, bool kFine = true>
 __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, float* st, TraceCounters* cnt) {
   constexpr bool kCount = kWalk == kWalkCount, kWide = kWalk == kWalkWide;
+  const bool any = kAny == kAnyRuntime ? tr.any : kAny == kAnyHit;
+  bool pop = false;
   if (kWide && tr.mode == kTravNode) {
-    if (!trav_node4(tr, s, sn, st)) {
+    const int r = trav_node4(tr, s, sn, st);
+    if (r == kStepOverflow) {
       flag_error(s, BN_DEVERR_STACK_OVERFLOW);
       tr.mode = kTravDone;
       return true;
     }
+    pop = r == kStepPop;
   } else if (tr.mode == kTravNode) {
     const Ray& r = tr.level ? tr.orr : tr.wr;
     const V3 inv = tr.level ? tr.oinv : tr.winv;
@@ -261,7 +268,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     } else if (hb) {
       trav_enter(tr, ri, b);
     } else {
-      trav_pop<kWide>(tr, s, sn, st);
+      pop = true;
     }
   } else if (tr.mode == kTravTri) {
     // one triangle of a BLAS leaf: its AABB pre-test (Mesh.fs:204,231), then the triangle test
@@ -279,7 +286,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
                          : tri_mt(p0, p1, p2, tr.orr, tr.t, &tt, &uu, &vv);
       if (h) {
         tr.found = true;
-        if (kAny) {
+        if (any) {
           tr.mode = kTravDone;
           return true;
         }
@@ -289,7 +296,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     }
     if (kFine) break;
     }
-    if (tr.ti >= tr.ti_end) trav_pop<kWide>(tr, s, sn, st);
+    pop = tr.ti >= tr.ti_end;
   } else if (tr.mode == kTravInst) {
     // one instance of a TLAS leaf (PrimitiveInstance.Intersect, Primitive.fs:111-129)
     bool entered = false;
@@ -308,7 +315,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
         const int root = sphere_hit(bmax.w, tr.orr, tr.t, &ts);
         if (root) {
           tr.found = true;
-          if (kAny) {
+          if (any) {
             tr.mode = kTravDone;
             return true;
           }
@@ -339,32 +346,55 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
       }
     }
     }
-    if (!entered && tr.ii >= tr.ii_end) trav_pop<kWide>(tr, s, sn, st);
+    pop = !entered && tr.ii >= tr.ii_end;
   }
+  if (pop) trav_pop<kWide>(tr, s, sn, st);
   return tr.mode == kTravDone;
 }
 
-template <bool kAny, bool kWT, int kWalk>
-__device__ __forceinline__ bool trace_walk(const DevScene& s, const Ray& ray, float tmax, HitRec* hit, TraceCounters* cnt) {
+// A walk, inlined at its call site with the query fixed at compile time.
+template <int kAny, bool kWT, int kWalk>
+__device__ __forceinline__ bool trace_walk_inline(const DevScene& s, const Ray& ray, float tmax, HitRec* hit,
+                                                  TraceCounters* cnt) {
   int sn[kStackSize];
   float st[kStackSize];
   Trav tr;
   trav_init<kWalk>(tr, s, ray, tmax, cnt);
   while (!trav_step<kAny, kWT, kWalk, false>(tr, s, sn, st, cnt)) {
   }
-  if (!kAny) *hit = tr.hit;
+  if (kAny == kClosest) *hit = tr.hit;
   return tr.found;
 }
 
+// One walk for both queries, kept out of line: a path loop that traces closest and any hits
+// then holds a single copy of the traversal code.  That keeps a large kernel whose time goes to
+// shading within the instruction cache; a kernel whose time goes to long walks keeps them
+// inlined, where the walk's registers are allocated with the loop around it.
 template <bool kWT, int kWalk>
-__device__ __forceinline__ bool trace_closest(const DevScene& s, const Ray& ray, float tmax, HitRec* hit, TraceCounters* cnt) {
-  return trace_walk<false, kWT, kWalk>(s, ray, tmax, hit, cnt);
+__device__ __noinline__ bool trace_walk_outline(const DevScene& s, const Ray& ray, float tmax, bool any, HitRec* hit,
+                                                TraceCounters* cnt) {
+  int sn[kStackSize];
+  float st[kStackSize];
+  Trav tr;
+  tr.any = any;
+  trav_init<kWalk>(tr, s, ray, tmax, cnt);
+  while (!trav_step<kAnyRuntime, kWT, kWalk, false>(tr, s, sn, st, cnt)) {
+  }
+  if (!any) *hit = tr.hit;
+  return tr.found;
 }
 
-template <bool kWT, int kWalk>
+template <bool kWT, int kWalk, bool kOutline = false>
+__device__ __forceinline__ bool trace_closest(const DevScene& s, const Ray& ray, float tmax, HitRec* hit, TraceCounters* cnt) {
+  if (kOutline) return trace_walk_outline<kWT, kWalk>(s, ray, tmax, false, hit, cnt);
+  return trace_walk_inline<kClosest, kWT, kWalk>(s, ray, tmax, hit, cnt);
+}
+
+template <bool kWT, int kWalk, bool kOutline = false>
 __device__ __forceinline__ bool trace_any(const DevScene& s, const Ray& ray, float tmax, TraceCounters* cnt) {
   HitRec h;
-  return trace_walk<true, kWT, kWalk>(s, ray, tmax, &h, cnt);
+  if (kOutline) return trace_walk_outline<kWT, kWalk>(s, ray, tmax, true, &h, cnt);
+  return trace_walk_inline<kAnyHit, kWT, kWalk>(s, ray, tmax, &h, cnt);
 }
 
 }  // namespace bn

@@ -119,7 +119,7 @@ __device__ V3 li_adj(const AdjParams& p, Ray ray, IndepSampler& smp, V3 L_total,
   TraceCounters tc;
   while (depth < p.max_depth) {
     HitRec h;
-    if (!trace_closest<false, kWalk>(s, ray, CUDART_INF_F, &h, &tc)) break;
+    if (!trace_closest<false, kWalk, true>(s, ray, CUDART_INF_F, &h, &tc)) break;
     const Interaction it = make_interaction(s, ray, h);
     const DevInstance* I = s.inst + it.inst;
     const int light = __ldg(&I->light);
@@ -153,7 +153,7 @@ __device__ V3 li_adj(const AdjParams& p, Ray ray, IndepSampler& smp, V3 L_total,
       Ray sh;
       sh.o = it.p;
       sh.d = ls.wi;
-      if (!trace_any<false, kWalk>(s, sh, __fsub_rn(dist, 1e-3f), &tc)) {
+      if (!trace_any<false, kWalk, true>(s, sh, __fsub_rn(dist, 1e-3f), &tc)) {
         const V3 wi = to_local(it.f, ls.wi);
         const BsdfEval bes = bsdf_eval(ms, wo, wi);
         const BsdfEval bev = slotted ? bsdf_eval(mv, wo, wi) : bes;

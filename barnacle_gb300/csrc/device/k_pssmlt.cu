@@ -212,23 +212,28 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
     m.stride = p.n_chains;
     m.max_dims = p.n_dims;
     PathCounters pc{};
-    m.start_iteration();
-    int px, py;
-    Ray ray = mlt_camera(v, m, &px, &py);
-    V3 L = li_path<kWT, true, kWalk>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
-    float y = luminance(L);
-    m.accept();
-    m.inner = xxhash32_three(static_cast<uint32_t>(chain), static_cast<uint32_t>(bid), static_cast<uint32_t>(p.frame_id));
     const float inv_b = __frcp_rn(p.b);
     const float inv_spp = p.inv_eff_spp;
-    V3 radiance = mk(0.f, 0.f, 0.f);
-    int pix = (H - py - 1) * W + px;
-    for (int it = 0; it < p.mutations_per_chain; ++it) {
+    V3 radiance = mk(0.f, 0.f, 0.f), L = mk(0.f, 0.f, 0.f);
+    float y = 0.f;
+    int pix = 0;
+    // iteration -1 evaluates the chain's starting path (the bootstrap sample it was drawn from);
+    // one call site of the path loop keeps the kernel's code small
+    for (int it = -1; it < p.mutations_per_chain; ++it) {
       m.start_iteration();
       int nx, ny;
-      ray = mlt_camera(v, m, &nx, &ny);
+      const Ray ray = mlt_camera(v, m, &nx, &ny);
       const V3 Ln = li_path<kWT, true, kWalk>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
       const float yn = luminance(Ln);
+      if (it < 0) {
+        L = Ln;
+        y = yn;
+        m.accept();
+        m.inner = xxhash32_three(static_cast<uint32_t>(chain), static_cast<uint32_t>(bid),
+                                 static_cast<uint32_t>(p.frame_id));
+        pix = (H - ny - 1) * W + nx;
+        continue;
+      }
       const float ratio = __fdiv_rn(yn, y);
       const float acc = ratio != ratio ? ratio : fminf(1.f, ratio);  // MathF.Min propagates NaN
       const float w_old = __fdiv_rn(__fsub_rn(1.f, acc), fmaf(y, inv_b, p.large_step_prob));

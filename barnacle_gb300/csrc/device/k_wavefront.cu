@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
       }
     }
     // a walk can end at init (root box missed)
-    if (have && (tr.mode == kTravDone || trav_step<false, kWT, kWalk>(tr, s, sn, st, &tc))) {
+    if (have && (tr.mode == kTravDone || trav_step<kClosest, kWT, kWalk>(tr, s, sn, st, &tc))) {
       have = false;
       pending = true;
     }
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict
         have = true;
       }
     }
-    if (have && (tr.mode == kTravDone || trav_step<true, kWT, kWalk>(tr, p.scene, sn, st, &tc))) {
+    if (have && (tr.mode == kTravDone || trav_step<kAnyHit, kWT, kWalk>(tr, p.scene, sn, st, &tc))) {
       have = false;
       pending = true;
     }

@@ -1,13 +1,14 @@
 """Benchmark of the render call on the 1,024-instance, 16-view workload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--mode wavefront|megakernel]
-                  [--impl reference] [--spp-per-step S]
+                  [--impl reference] [--spp-per-step S] [--workload instances|cornell]
 
 A step renders every one of the 16 views (256x240 ... 1920x1080, ~13 M pixels) at S samples per
 pixel (the workload's 64 spp = 64 / S steps), max depth 12, Russian roulette from depth 3, the
 alias-table light sampler over the 64 emissive triangles.  The scene (630 k unique / 163 M
 instanced triangles, 1,089 instances) is resident in HBM; L2 is flushed (a 512 MiB write)
-before every timed step.
+before every timed step.  --workload cornell times the Cornell box instead (256x256, one
+64-spp render per step, depth 8).
 
 value  = paths / device time (CUDA events on the library's stream around its kernels).
 e2e    = the same metric through bn_render with a host output buffer: the views' descriptors
@@ -38,7 +39,13 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "paths/sec at equal image RMSE: batched wavefront vs plain megakernel; adjoint/fwd"
-WORKLOAD = "instances"
+# name -> (description, samples per pixel per step, CPU sample: views, crop, spp)
+WORKLOADS = {
+    "instances": ("instances: 1024 instances of 4 displaced icospheres (20k/82k/200k/328k tris) + 64 emissive "
+                  "triangles, 16 views 256x240..1920x1080, depth 12, rr 3", 4, (4, 128, 24)),
+    "cornell": ("cornell: procedural Cornell box (24 triangles, two rotated boxes, ceiling light), 256x256, "
+                "depth 8", 64, (1, 96, 64)),
+}
 
 
 def bytes_per_unit():
@@ -225,12 +232,12 @@ def run_reference(args, world, rank, dist):
         return
     from barnacle_gb300 import Bundle
 
-    b = Bundle.generate(WORKLOAD, 1)
+    b = Bundle.generate(args.workload, 1)
     views = b.views
     threads = os.cpu_count() or 1
     r = b.render
     sample_views = views[:4]
-    crop = 48
+    crop = 48 if args.workload == "instances" else 32
     for _ in range(args.warmup):
         cpu_sample_render(b, b.render, args.spp_per_step, sample_views[:1], 16, threads)
     paths, secs = 0, 0.0
@@ -243,12 +250,12 @@ def run_reference(args, world, rank, dist):
             "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
             "impl": "reference",
-            "config": {"workload": f"{WORKLOAD}: 1024 instances of 4 displaced icospheres + 64 emissive triangles, "
-                                   "16 views, depth 12, rr 3", "spp_per_step": args.spp_per_step,
+            "config": {"workload": WORKLOADS[args.workload][0], "spp_per_step": args.spp_per_step,
                        "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
-                             "sample": f"{crop}x{crop} centre crops of 4 of the 16 views x {args.spp_per_step} spp "
-                                       f"per step (the F# reference cannot be built: no .NET SDK)"},
+                             "sample": f"{crop}x{crop} centre crops of the first {len(sample_views)} view(s) x "
+                                       f"{args.spp_per_step} spp per step (the F# reference cannot be built: no "
+                                       f".NET SDK)"},
             "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -261,7 +268,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="wavefront", choices=["megakernel", "wavefront"])
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other render form")
-    ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--workload", default="instances", choices=sorted(WORKLOADS))
+    ap.add_argument("--spp-per-step", type=int, default=0, help="0 = the workload's default (instances 4, cornell 64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the Cornell-box CPU ratio, PSSMLT and adjoint/forward measurements")
@@ -273,6 +281,8 @@ def main():
                     help="wavefront bounce loop driven from the host (ncu cannot profile kernels inside a "
                          "graph with a conditional node)")
     args = ap.parse_args()
+    if args.spp_per_step <= 0:
+        args.spp_per_step = WORKLOADS[args.workload][1]
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
@@ -283,7 +293,7 @@ def main():
 
     dev = local if world > 1 else 0
     ctx = Context(dev)
-    b = Bundle.generate(WORKLOAD, 1)
+    b = Bundle.generate(args.workload, 1)
     b.scene.contents.bvh_width = args.bvh_width
     ctx.upload(b)
     views = b.views
@@ -361,16 +371,17 @@ def main():
     dom_launch_s = dom_ms / 1000.0 / args.steps
     achieved = alg_bytes / dom_launch_s / 1e9
     traffic = None
-    prof = ROOT / "profiles" / f"traffic_{args.mode}_{WORKLOAD}.json"
+    prof = ROOT / "profiles" / f"traffic_{args.mode}_{args.workload}.json"
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("bytes_per_launch")
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        p, s = cpu_sample_render(b, b.render, 24, views[:4], 128, threads)
+        nv, crop, spp = WORKLOADS[args.workload][2]
+        p, s = cpu_sample_render(b, b.render, spp, views[:nv], crop, threads)
         cpu = {"value": p / s, "unit": "paths/s", "cores": threads, "kind": "port",
-               "sample": "128x128 centre crops of 4 of the 16 views x 24 spp "
+               "sample": f"{crop}x{crop} centre crops of the first {nv} view(s) x {spp} spp "
                          "(oracle: CPU restatement of the F# path; the F# renderer cannot be built here)"}
 
     extras = None
@@ -383,8 +394,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * dev_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": f"{WORKLOAD}: 1024 instances of 4 displaced icospheres (20k/82k/200k/328k tris) "
-                                   "+ 64 emissive triangles, 16 views 256x240..1920x1080, depth 12, rr 3",
+            "config": {"workload": WORKLOADS[args.workload][0],
                        "mode": args.mode, "bvh_width": {0: "auto", 2: "binary", 4: "wide"}[args.bvh_width], "spp_per_step": r.spp, "pixels_per_step": pixels,
                        "rays_per_step": int(rays_per_step),
                        "per_ray": {"nodes": st.nodes_visited / max(1, st.rays), "triangles": st.tris_tested / max(1, st.rays),
