@@ -81,6 +81,11 @@ class Bundle:
     def emissive_slot_base(self) -> int:
         return int(self._info.emissive_slot_base)
 
+    @property
+    def tone_mapping(self) -> int:
+        """capi.BN_TONE_*: the film's tone mapping (JSON "tone-mapping", ACES for procedural scenes)."""
+        return int(self._info.tone_mapping)
+
     def slot_params(self) -> np.ndarray | None:
         if self.n_slots == 0:
             return None
@@ -173,6 +178,21 @@ class Context:
     def film_download(self, out: np.ndarray) -> None:
         self._check(self.lib.bn_film_download(self._h, ptr(out), out.size))
 
+    def tonemap(self, tone_mapping: int, views) -> list:
+        """Film.PostProcess + 8-bit packing of the last render's film on the device: one
+        (H, W, 4) uint8 RGBA image per view (rows top to bottom, as Film.Save writes them)."""
+        if isinstance(views, capi.bn_view):
+            views = [views]
+        n = sum(v.width * v.height for v in views)
+        out = np.zeros(n * 4, np.uint8)
+        self._check(self.lib.bn_film_tonemap(self._h, tone_mapping, ptr(out), n))
+        imgs, off = [], 0
+        for v in views:
+            k = v.width * v.height * 4
+            imgs.append(out[off:off + k].reshape(v.height, v.width, 4))
+            off += k
+        return imgs
+
     def stats(self) -> capi.bn_stats:
         s = capi.bn_stats()
         self._check(self.lib.bn_get_stats(self._h, C.byref(s)))
@@ -218,3 +238,12 @@ def mat4_invert(m: np.ndarray) -> np.ndarray:
     out = np.zeros(16, np.float32)
     capi.load_library().bn_mat4_invert(ptr(m), ptr(out))
     return out
+
+
+def write_png(path: str, rgba: np.ndarray) -> None:
+    """An (H, W, 4) uint8 image as a PNG file."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    h, w = img.shape[:2]
+    rc = capi.load_library().bn_image_write_png(str(path).encode(), ptr(img), w, h)
+    if rc:
+        raise BarnacleError(rc, capi.host_error())

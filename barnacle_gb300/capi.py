@@ -26,8 +26,9 @@ BN_MAT_LAMBERTIAN, BN_MAT_MIRROR, BN_MAT_DIELECTRIC, BN_MAT_PBR = 0, 1, 2, 3
 BN_CAM_PINHOLE, BN_CAM_THIN_LENS = 0, 1
 BN_LIGHTS_UNIFORM, BN_LIGHTS_ALIAS_TRIANGLES = 0, 1
 BN_BVH_AUTO, BN_BVH_BINARY, BN_BVH_WIDE = 0, 2, 4
+BN_TONE_IDENTITY, BN_TONE_ACES, BN_TONE_GAMMA = 0, 1, 2
 BN_TRACE_CLOSEST, BN_TRACE_ANY, BN_TRACE_WATERTIGHT, BN_TRACE_COUNT = 0x0, 0x1, 0x2, 0x4
-BN_INTEGRATOR_PATH, BN_INTEGRATOR_PSSMLT = 0, 1
+BN_INTEGRATOR_PATH, BN_INTEGRATOR_PSSMLT, BN_INTEGRATOR_NORMAL, BN_INTEGRATOR_DIRECT = 0, 1, 2, 3
 BN_MODE_MEGAKERNEL, BN_MODE_WAVEFRONT = 0, 1
 BN_MUTATION_GAUSSIAN, BN_MUTATION_KELEMEN = 0, 1
 BN_RENDER_WATERTIGHT, BN_RENDER_FIXED_ALIAS, BN_RENDER_NO_GRAPH, BN_RENDER_COUNT = 0x1, 0x2, 0x4, 0x8
@@ -127,7 +128,8 @@ class bn_bundle_info(C.Structure):
     _fields_ = [("scene", C.POINTER(bn_scene_desc)), ("views", C.POINTER(bn_view)), ("n_views", C.c_int32),
                 ("render", bn_render_desc), ("n_triangles_unique", C.c_int64),
                 ("n_triangles_instanced", C.c_int64), ("n_material_slots", C.c_int32),
-                ("emissive_slot_base", C.c_int32), ("slot_params", C.POINTER(C.c_float))]
+                ("emissive_slot_base", C.c_int32), ("slot_params", C.POINTER(C.c_float)),
+                ("tone_mapping", C.c_int32)]
 
 
 # numpy dtypes matching the C structures (for bulk arrays)
@@ -160,6 +162,8 @@ SIGNATURES = {
     "bn_sampler_stream": (C.c_int, [P, P, C.c_int64, C.c_int32, P]),
     "bn_render": (C.c_int, [P, C.POINTER(bn_render_desc), C.POINTER(bn_view), C.c_int32, P]),
     "bn_film_download": (C.c_int, [P, P, C.c_int64]),
+    "bn_film_tonemap": (C.c_int, [P, C.c_int32, P, C.c_int64]),
+    "bn_image_write_png": (C.c_int, [C.c_char_p, P, C.c_int32, C.c_int32]),
     "bn_render_noalloc": (C.c_int, [P, C.POINTER(bn_render_desc), C.POINTER(bn_view), C.c_int32, P]),
     "bn_get_stats": (C.c_int, [P, C.POINTER(bn_stats)]),
     "bn_reset_stats": (C.c_int, [P]),

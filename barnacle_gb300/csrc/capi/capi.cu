@@ -94,6 +94,7 @@ int render_megakernel(bn_context* ctx, const bn_render_desc* d, const std::vecto
   p.max_depth = d->max_depth;
   p.rr_depth = d->rr_depth;
   p.frame_id = d->frame_id;
+  p.integrator = d->integrator;
   p.watertight = d->flags & BN_RENDER_WATERTIGHT;
   p.count = count;
   p.partial = ctx->partial.as<float4>();
@@ -148,7 +149,7 @@ int bn_destroy(bn_context* ctx) {
   if (!ctx) return BN_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf* bufs[] = {&ctx->nodes, &ctx->tris, &ctx->inst, &ctx->mats, &ctx->lights, &ctx->light_inst,
+  DevBuf* bufs[] = {&ctx->nodes, &ctx->nodes4, &ctx->rgba, &ctx->tris, &ctx->inst, &ctx->mats, &ctx->lights, &ctx->light_inst,
                     &ctx->tri_pdf, &ctx->tri_lights, &ctx->error_word, &ctx->counters, &ctx->q_in, &ctx->q_out,
                     &ctx->views, &ctx->item_offsets, &ctx->partial, &ctx->film, &ctx->wf_state, &ctx->mlt_state,
                     &ctx->mlt_boot, &ctx->mlt_chain, &ctx->adj_params, &ctx->adj_image, &ctx->adj_target,
@@ -286,7 +287,8 @@ int bn_render(bn_context* ctx, const bn_render_desc* d, const bn_view* views, in
   int rc;
   if (d->integrator == BN_INTEGRATOR_PSSMLT) {
     rc = bnc::render_pssmlt(ctx, d, dv);
-  } else if (d->integrator == BN_INTEGRATOR_PATH) {
+  } else if (d->integrator == BN_INTEGRATOR_PATH || d->integrator == BN_INTEGRATOR_NORMAL ||
+             d->integrator == BN_INTEGRATOR_DIRECT) {
     if (d->mode == BN_MODE_WAVEFRONT) rc = bnc::render_wavefront(ctx, d, dv);
     else if (d->mode == BN_MODE_MEGAKERNEL) rc = render_megakernel(ctx, d, dv, count);
     else return ctx->fail(BN_ERR_INVALID_ARG, "unknown render mode");
@@ -319,6 +321,23 @@ int bn_film_download(bn_context* ctx, float* out_rgb, int64_t n_floats) {
   cudaError_t e = cudaMemcpyAsync(out_rgb, ctx->film.ptr, n_floats * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return e == cudaSuccess ? BN_OK : ctx->cuda_fail(e, "film download");
+}
+
+int bn_film_tonemap(bn_context* ctx, int32_t tone_mapping, uint8_t* rgba, int64_t n_pixels) {
+  if (!ctx || !rgba) return BN_ERR_INVALID_ARG;
+  if (tone_mapping != BN_TONE_IDENTITY && tone_mapping != BN_TONE_ACES && tone_mapping != BN_TONE_GAMMA)
+    return ctx->fail(BN_ERR_INVALID_ARG, "bn_film_tonemap: unknown tone mapping");
+  if (n_pixels <= 0 || 3 * n_pixels > ctx->film_floats)
+    return ctx->fail(BN_ERR_INVALID_ARG, "bn_film_tonemap: n_pixels must be 1 .. the last render's film pixels");
+  cudaSetDevice(ctx->device);
+  cudaError_t e = ctx->rgba.reserve(static_cast<size_t>(n_pixels) * 4);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "alloc tone-mapped film");
+  if ((e = bn::launch_film_tonemap(ctx->film.as<float>(), n_pixels, tone_mapping, ctx->rgba.ptr, ctx->stream)) !=
+      cudaSuccess)
+    return ctx->cuda_fail(e, "tone-map launch");
+  e = cudaMemcpyAsync(rgba, ctx->rgba.ptr, static_cast<size_t>(n_pixels) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return e == cudaSuccess ? BN_OK : ctx->cuda_fail(e, "tone-mapped film download");
 }
 
 int bn_get_stats(const bn_context* ctx, bn_stats* out) {

@@ -51,7 +51,7 @@ struct bn_context {
   DevBuf q_in, q_out;
 
   // render
-  DevBuf views, item_offsets, partial, film, wf_state;
+  DevBuf views, item_offsets, partial, film, wf_state, rgba;
   long long film_floats = 0;
   bn_stats stats{};
 

@@ -139,6 +139,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.max_depth = d->max_depth;
   p.rr_depth = d->rr_depth;
   p.frame_id = d->frame_id;
+  p.integrator = d->integrator;
   p.pool = pool;
   // refill thresholds (lanes of 32 still walking), measured on the 1,024-instance workload: 16-24
   // are within 0.5% of each other; 31 (refill as soon as one lane is free) is 19% slower, 0 11%

@@ -378,6 +378,11 @@ __device__ __forceinline__ int hit_material(const DevScene& s, const Interaction
   return slot >= 0 ? slot : m;
 }
 
+// 0.5 * (n + Vector3.One), the Normal integrator's colour
+__device__ __forceinline__ V3 normal_color(V3 n) {
+  return {__fmul_rn(0.5f, __fadd_rn(n.x, 1.f)), __fmul_rn(0.5f, __fadd_rn(n.y, 1.f)), __fmul_rn(0.5f, __fadd_rn(n.z, 1.f))};
+}
+
 struct PathCounters {
   unsigned long long rays;
   TraceCounters tc;
@@ -443,6 +448,64 @@ __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int 
       else break;
     }
     depth++;
+  }
+  return L;
+}
+
+// NormalIntegrator.Li (Extensions/Integrator/Normal.fs:10-17): 0.5 (n + 1) of the shading normal
+template <bool kWT, int kWalk, bool kOutline = false>
+__device__ __forceinline__ V3 li_normal(const DevScene& s, Ray ray, PathCounters* pc) {
+  HitRec h;
+  if (kWalk == kWalkCount) pc->rays++;
+  if (!trace_closest<kWT, kWalk, kOutline>(s, ray, CUDART_INF_F, &h, &pc->tc)) return mk(0.f, 0.f, 0.f);
+  const Interaction it = make_interaction(s, ray, h);
+  return normal_color(it.f.n);
+}
+
+// DirectIntegrator.Li (Extensions/Integrator/Direct.fs:10-40): emission seen directly (weight 1),
+// one light sample weighted 1/pdf_light, and one BSDF sample that scores the light it hits with
+// f / pdf_light (the reference divides by the light's pdf, not the BSDF's, and checks neither
+// pdf for zero).  Draw order: u_select, u_light.xy, u_lobe, u_bsdf.xy.
+template <bool kWT, int kWalk, class Smp, bool kOutline = false>
+__device__ __forceinline__ V3 li_direct(const DevScene& s, Ray ray, Smp& smp, PathCounters* pc) {
+  constexpr bool kCount = kWalk == kWalkCount;
+  V3 L = mk(0.f, 0.f, 0.f);
+  HitRec h;
+  if (kCount) pc->rays++;
+  if (!trace_closest<kWT, kWalk, kOutline>(s, ray, CUDART_INF_F, &h, &pc->tc)) return L;
+  const Interaction it = make_interaction(s, ray, h);
+  const V3 wo_w = neg(ray.d);
+  const int light = __ldg(&s.inst[it.inst].light);
+  if (light >= 0) L = add(L, light_le(s.lights[light], dot(wo_w, it.f.n)));  // EvalEmit(-d)
+  const int mat = hit_material(s, it);
+  if (mat < 0) return L;
+  const float u_sel = smp.next(), ulx = smp.next(), uly = smp.next();
+  const DevMaterial m = s.mats[mat];
+  const LightSample ls = sample_light(s, it.p, u_sel, ulx, uly);
+  const float dist = length(sub(ls.p, it.p));
+  Ray sh;
+  sh.o = it.p;
+  sh.d = ls.wi;
+  if (kCount) pc->rays++;
+  if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
+    const BsdfEval be = bsdf_eval(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
+    L = fma3(be.f, scale(__frcp_rn(ls.pdf), ls.L), L);
+  }
+  const float u_lobe = smp.next(), ubx = smp.next(), uby = smp.next();
+  const BsdfSample bs = bsdf_sample(m, to_local(it.f, wo_w), u_lobe, ubx, uby);
+  Ray r2;
+  r2.o = it.p;
+  r2.d = to_world(it.f, bs.wi);
+  HitRec h2;
+  if (kCount) pc->rays++;
+  if (trace_closest<kWT, kWalk, kOutline>(s, r2, CUDART_INF_F, &h2, &pc->tc)) {
+    const Interaction it2 = make_interaction(s, r2, h2);
+    if (__ldg(&s.inst[it2.inst].light) >= 0) {
+      V3 le;
+      float pdf_l;
+      eval_light(s, r2.o, it2, &le, &pdf_l);
+      L = fma3(bs.f, scale(__frcp_rn(pdf_l), le), L);
+    }
   }
   return L;
 }

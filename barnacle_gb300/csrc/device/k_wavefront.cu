@@ -120,7 +120,8 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
         p.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
         const long long film_pix = v.pixel_offset + static_cast<long long>(v.height - y - 1) * v.width + x;
         m = make_int4(static_cast<int>(film_pix), 0, static_cast<int>(smp.state), kStatusActive);
-        if (p.max_depth <= 0) m.w = kStatusDone;  // while (depth < maxDepth) never runs
+        // PathTracing: while (depth < maxDepth) never runs; Normal and Direct ignore maxDepth
+        if (p.max_depth <= 0 && p.integrator == BN_INTEGRATOR_PATH) m.w = kStatusDone;
       }
     }
     const bool active = valid && m.w == kStatusActive;
@@ -214,6 +215,55 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
   }
 }
 
+// DirectIntegrator.Li (Extensions/Integrator/Direct.fs:10-40) as two wavefront vertices.  At the
+// camera hit: emission seen directly (EvalEmit(-d)), a shadow record for one light sample (a = f,
+// b = L_light / pdf_light; the shadow kernel adds fma(a, b, L) if unoccluded, as the reference's
+// FusedMultiplyAdd), and a BSDF sample that always continues with beta = f.  At the second hit:
+// a light scores fma(beta, Le / pdf_light, L); the path ends either way.
+__device__ __forceinline__ void shade_direct(const WfParams& p, const DevScene& s, int slot, const Ray& ray,
+                                             const Interaction& it, int depth, IndepSampler& smp, V3* beta, V3* L,
+                                             bool* done, bool* cont, bool* shadow, float4* sh_o, float4* sh_d,
+                                             float4* sh_a, float4* sh_b) {
+  const int light = __ldg(&s.inst[it.inst].light);
+  if (depth > 0) {
+    if (light >= 0) {
+      V3 le;
+      float pdf_l;
+      eval_light(s, ray.o, it, &le, &pdf_l);
+      *L = fma3(*beta, scale(__frcp_rn(pdf_l), le), *L);
+    }
+    *done = true;
+    return;
+  }
+  const V3 wo_w = neg(ray.d);
+  if (light >= 0) *L = add(*L, light_le(s.lights[light], dot(wo_w, it.f.n)));
+  const int mat = hit_material(s, it);
+  if (mat < 0) {
+    *done = true;
+    return;
+  }
+  const float u_sel = smp.next(), ulx = smp.next(), uly = smp.next();
+  const DevMaterial mt = s.mats[mat];
+  const LightSample ls = sample_light(s, it.p, u_sel, ulx, uly);
+  const float dist = length(sub(ls.p, it.p));
+  const BsdfEval be = bsdf_eval(mt, to_local(it.f, wo_w), to_local(it.f, ls.wi));
+  const V3 bb = scale(__frcp_rn(ls.pdf), ls.L);
+  *sh_o = make_float4(it.p.x, it.p.y, it.p.z, __fsub_rn(dist, 1e-3f));
+  *sh_d = make_float4(ls.wi.x, ls.wi.y, ls.wi.z, __int_as_float(slot));
+  *sh_a = make_float4(be.f.x, be.f.y, be.f.z, 0.f);
+  *sh_b = make_float4(bb.x, bb.y, bb.z, 0.f);
+  *shadow = true;
+  const float u_lobe = smp.next(), ubx = smp.next(), uby = smp.next();
+  const BsdfSample bs = bsdf_sample(mt, to_local(it.f, wo_w), u_lobe, ubx, uby);
+  const V3 nd = to_world(it.f, bs.wi);
+  *beta = bs.f;
+  p.ray_o[slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
+  p.ray_d[slot] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
+  p.beta[slot] = make_float4(bs.f.x, bs.f.y, bs.f.z, 0.f);
+  if (p.sort) p.slot_key[slot] = ray_key(p, it.p, nd);
+  *cont = true;
+}
+
 template <bool kWT>
 __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
@@ -255,6 +305,14 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
         V3 L = mk(L4.x, L4.y, L4.z);
         const int depth = m.y;
         const DevInstance* I = s.inst + it.inst;
+        IndepSampler smp{static_cast<uint32_t>(m.z)};
+        if (p.integrator == BN_INTEGRATOR_NORMAL) {
+          L = normal_color(it.f.n);
+          done = true;
+        } else if (p.integrator == BN_INTEGRATOR_DIRECT) {
+          shade_direct(p, s, slot, ray, it, depth, smp, &beta, &L, &done, &cont, &shadow, &sh_o, &sh_d, &sh_a, &sh_b);
+          if (cont) m.y = 1;
+        } else {
         if (__ldg(&I->light) >= 0) {
           V3 le;
           float pdf_l;
@@ -263,7 +321,6 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
           L = fma3(beta, scale(mis, le), L);
         }
         const int mat = hit_material(s, it);
-        IndepSampler smp{static_cast<uint32_t>(m.z)};
         if (mat < 0) {
           done = true;
         } else {
@@ -306,6 +363,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
               done = true;
             }
           }
+        }
         }
         p.L[slot] = make_float4(L.x, L.y, L.z, 0.f);
         m.z = static_cast<int>(smp.state);

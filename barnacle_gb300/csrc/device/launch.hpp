@@ -54,6 +54,7 @@ struct MegaParams {
   const long long* item_offsets;  // per view: first item (device)
   int spp, chunks, spc;      // samples per pixel, chunks per pixel, samples per chunk
   int max_depth, rr_depth, frame_id;
+  int integrator;            // bn_integrator_type: PATH, NORMAL or DIRECT
   bool watertight;
   bool count;
   float4* partial;           // n_items partial sums (scratch)
@@ -62,6 +63,10 @@ struct MegaParams {
   DevCounters* counters;
 };
 cudaError_t launch_megakernel(const DevScene& s, const MegaParams& p, cudaStream_t st);
+cudaError_t launch_megakernel_simple(const DevScene& s, const MegaParams& p, cudaStream_t st);  // NORMAL, DIRECT
 cudaError_t launch_mega_reduce(const MegaParams& p, cudaStream_t st);
+
+// Film.PostProcess + Rgba32 packing over n_pixels RGB floats into 4-byte RGBA
+cudaError_t launch_film_tonemap(const float* film, long long n_pixels, int tone_mapping, void* rgba, cudaStream_t st);
 
 }  // namespace bn

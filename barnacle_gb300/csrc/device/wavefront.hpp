@@ -29,6 +29,7 @@ struct WfParams {
   const DevView* views;
   int n_views;
   int spp, max_depth, rr_depth, frame_id;
+  int integrator;               // BN_INTEGRATOR_PATH, _NORMAL or _DIRECT
   int pool;                     // path slots
   int max_iters;                // watchdog
   int refill_extend;            // extend lanes refill when at most this many of a warp still walk

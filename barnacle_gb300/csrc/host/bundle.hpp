@@ -22,6 +22,7 @@ struct bn_scene_bundle {
   bn_scene_desc scene{};
   bn_render_desc render{};
   int32_t light_sampler = BN_LIGHTS_UNIFORM;
+  int32_t tone_mapping = BN_TONE_ACES;
   int32_t n_slots = 0;
   int32_t emissive_slot_base = 0;
   std::vector<float> slot_params;

@@ -14,6 +14,9 @@ int host_fail(int code, const std::string& msg) {
 }
 }  // namespace
 
+// the error channel of bn_host_last_error, for host helpers in other files (png.cpp)
+int bnh_host_fail(int code, const std::string& msg) { return host_fail(code, msg); }
+
 extern "C" {
 
 int bn_host_last_error(char* buf, size_t len) {
@@ -80,6 +83,7 @@ int bn_bundle_info_get(const bn_scene_bundle* b, bn_bundle_info* out) {
   out->n_material_slots = b->n_slots;
   out->emissive_slot_base = b->emissive_slot_base;
   out->slot_params = b->slot_params.empty() ? nullptr : b->slot_params.data();
+  out->tone_mapping = b->tone_mapping;
   return BN_OK;
 }
 

@@ -380,9 +380,10 @@ bool load_json_bundle(const std::string& path, bn_scene_bundle* b, std::string* 
     else if (ms == "Kelemen") { r.mutation = BN_MUTATION_KELEMEN; r.eps_min = 1.f / 1024.f; r.eps_max = 1.f / 16.f; }
     else { *err = "Unknown mutation strategy: " + ms; return false; }
     r.large_step_prob = fnum(ig->get("large-step-prob"), 0.5f);
-  } else if (itype == "normal" || itype == "direct") {
-    *err = "integrator '" + itype + "' has no GPU implementation in this library";
-    return false;
+  } else if (itype == "normal") {
+    r.integrator = BN_INTEGRATOR_NORMAL;   // NormalIntegrator(spp) (Loader.fs:186)
+  } else if (itype == "direct") {
+    r.integrator = BN_INTEGRATOR_DIRECT;   // DirectIntegrator(spp) (Loader.fs:187)
   } else {
     *err = "Unknown integrator type: " + itype;
     return false;
@@ -404,7 +405,10 @@ bool load_json_bundle(const std::string& path, bn_scene_bundle* b, std::string* 
   const JVal* fj = root.get("film");
   if (!fj) { *err = "scene has no film"; return false; }
   const std::string tm = jstr(fj->get("tone-mapping"));
-  if (tm != "aces" && tm != "gamma" && tm != "identity") { *err = "Unknown tone mapping type: " + tm; return false; }
+  if (tm == "aces") b->tone_mapping = BN_TONE_ACES;
+  else if (tm == "gamma") b->tone_mapping = BN_TONE_GAMMA;
+  else if (tm == "identity") b->tone_mapping = BN_TONE_IDENTITY;
+  else { *err = "Unknown tone mapping type: " + tm; return false; }
   view.width = inum(fj->get("width"), 0);
   view.height = inum(fj->get("height"), 0);
   if (view.width <= 0 || view.height <= 0) { *err = "film width/height must be positive"; return false; }

@@ -163,7 +163,13 @@ typedef struct bn_bsdf_result {
 } bn_bsdf_result;
 
 /* ---- render (Base/Integrator.fs:22-55, PathTracing.fs, PSSMLT.fs) ---------------------- */
-enum bn_integrator_type { BN_INTEGRATOR_PATH = 0, BN_INTEGRATOR_PSSMLT = 1 };
+enum bn_integrator_type {
+  BN_INTEGRATOR_PATH = 0,   /* PathTracingIntegrator (Extensions/Integrator/PathTracing.fs)        */
+  BN_INTEGRATOR_PSSMLT = 1, /* PSSMLTIntegrator (Extensions/Integrator/PSSMLT.fs)                  */
+  BN_INTEGRATOR_NORMAL = 2, /* NormalIntegrator (Extensions/Integrator/Normal.fs): 0.5 (n + 1)     */
+  BN_INTEGRATOR_DIRECT = 3  /* DirectIntegrator (Extensions/Integrator/Direct.fs): one light sample */
+                            /* and one BSDF sample that scores a light it hits                     */
+};
 enum bn_render_mode {
   BN_MODE_MEGAKERNEL = 0, /* one thread per pixel-sample path, the plain form           */
   BN_MODE_WAVEFRONT = 1   /* persistent queues compacted every bounce, many views/launch */
@@ -184,7 +190,7 @@ typedef struct bn_view {
 
 typedef struct bn_render_desc {
   int32_t integrator;        /* bn_integrator_type                                   */
-  int32_t mode;              /* bn_render_mode (path tracing only)                   */
+  int32_t mode;              /* bn_render_mode (path, normal and direct integrators)  */
   int32_t spp;               /* samples per pixel, or PSSMLT mutations per pixel     */
   int32_t max_depth;         /* default 8                                            */
   int32_t rr_depth;          /* default 5                                            */
@@ -252,6 +258,18 @@ int bn_sampler_stream(bn_context* ctx, const uint32_t* seeds, int64_t n_streams,
 int bn_render(bn_context* ctx, const bn_render_desc* desc, const bn_view* views, int32_t n_views,
               float* out_rgb);
 int bn_film_download(bn_context* ctx, float* out_rgb, int64_t n_floats);
+
+/* Film output (Base/Film.fs:21-30 PostProcess, :55-66 Save).  bn_film_tonemap maps the film of the
+ * last bn_render on the device — identity, ACES fit x(2.51x+0.03)/(x(2.43x+0.59)+0.14) or gamma
+ * x^(1/2.2), clamped to [0, 1] — and packs it as ImageSharp's Rgba32(Vector3) does
+ * (byte = clamp(255 v + 0.5, 0, 255) truncated; NaN -> 0; alpha 255).  rgba receives 4 bytes per
+ * pixel in Film.Pixels order (rows top to bottom) for the first n_pixels of the film (the views
+ * one after another; the film's total for all of them). */
+enum bn_tone_mapping { BN_TONE_IDENTITY = 0, BN_TONE_ACES = 1, BN_TONE_GAMMA = 2 };
+int bn_film_tonemap(bn_context* ctx, int32_t tone_mapping, uint8_t* rgba, int64_t n_pixels);
+/* PNG encoding of an RGBA8 image (the encoder Film.Save hands to ImageSharp; stored deflate
+ * blocks, so no compression library is needed). */
+int bn_image_write_png(const char* path, const uint8_t* rgba, int32_t width, int32_t height);
 
 /* Render without allocating device memory (no counterpart in the reference).
  * For callers that cannot allocate during a render: a host whose device memory all comes from
@@ -328,6 +346,8 @@ typedef struct bn_bundle_info {
   int32_t n_material_slots;       /* differentiable workload: slots, else 0 */
   int32_t emissive_slot_base;
   const float* slot_params;       /* n_material_slots * 6 ground-truth params, or NULL */
+  int32_t tone_mapping;           /* bn_tone_mapping of the film (JSON "tone-mapping"; ACES for the
+                                     procedural workloads, as the reference's sample images) */
 } bn_bundle_info;
 
 /* name: "cornell" (256^2 64spp d8), "cornell-objects" (512^2 256spp d16, icospheres + mirror),

@@ -30,6 +30,7 @@ def lib() -> C.CDLL:
             "or_bvh_build": (C.c_int, [P, C.c_int32, P, P, P]),
             "or_trace": (C.c_int, [P, P, C.c_int64, C.c_uint32, P, P]),
             "or_sampler_stream": (C.c_int, [P, C.c_int64, C.c_int32, P]),
+            "or_tonemap": (C.c_int, [P, C.c_int64, C.c_int32, P]),
             "or_xxhash32_two": (C.c_uint32, [C.c_uint32, C.c_uint32]),
             "or_xxhash32_three": (C.c_uint32, [C.c_uint32, C.c_uint32, C.c_uint32]),
             "or_bsdf": (C.c_int, [P, P, C.c_int64, C.c_int, C.c_int, P]),
@@ -62,6 +63,15 @@ def sampler_stream(seeds: np.ndarray, n_draws: int) -> np.ndarray:
     s = np.ascontiguousarray(seeds, np.uint32).reshape(-1, 3)
     out = np.zeros((len(s), n_draws), np.float32)
     lib().or_sampler_stream(ptr(s), len(s), n_draws, ptr(out))
+    return out
+
+
+def tonemap(rgb: np.ndarray, tone_mapping: int) -> np.ndarray:
+    """Film.PostProcess + Rgba32 packing: (..., 3) float32 -> (..., 4) uint8."""
+    x = np.ascontiguousarray(rgb, np.float32)
+    out = np.zeros(x.shape[:-1] + (4,), np.uint8)
+    if lib().or_tonemap(ptr(x), x.size // 3, tone_mapping, ptr(out)):
+        raise ValueError("unknown tone mapping")
     return out
 
 

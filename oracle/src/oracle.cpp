@@ -1030,6 +1030,50 @@ Vector3 Li(const Scene& sc, Ray ray, Smp& smp, int maxDepth, int rrDepth, bool w
   return L;
 }
 
+// NormalIntegrator.Li (Extensions/Integrator/Normal.fs:10-17)
+Vector3 LiNormal(const Scene& sc, const Ray& ray, bool wt, Counters* c) {
+  float t = kInf;
+  Interaction it;
+  if (!sc.Closest(ray, &t, &it, wt, c)) return Vector3(0.f);
+  return 0.5f * (it.geom.onb.n + Vector3(1.f));
+}
+
+// DirectIntegrator.Li (Extensions/Integrator/Direct.fs:10-40).  Neither pdf is checked for zero,
+// and the BSDF-sampled hit is weighted by the light's pdf, as in the reference.
+template <class Smp>
+Vector3 LiDirect(const Scene& sc, const Ray& ray, Smp& smp, bool wt, Counters* c) {
+  float t = kInf;
+  Interaction it;
+  Vector3 L(0.f);
+  if (!sc.Closest(ray, &t, &it, wt, c)) return L;
+  const Instance& I = sc.inst[it.inst];
+  if (I.light >= 0) L = L + sc.lights[I.light].Eval(it.geom.onb.WorldToLocal(-ray.Direction));
+  const int mat = sc.HitMaterial(it);
+  if (mat < 0) return L;
+  const float uSel = smp.next(), ulx = smp.next(), uly = smp.next();
+  const Scene::LightSample ls = sc.SampleLight(it.geom.p, uSel, ulx, uly);
+  const Ray sh{it.geom.p, ls.wi};
+  const float dist = (ls.p - it.geom.p).Length();
+  const MaterialF& m = sc.mats[mat];
+  const Vector3 wo = -ray.Direction;
+  if (!sc.Any(sh, dist - 1e-3f, wt, c)) {
+    const BSDFEvalT<float> be = m.Eval(it.geom.onb.WorldToLocal(wo), it.geom.onb.WorldToLocal(ls.wi));
+    L = Vector3::FusedMultiplyAdd(be.bsdf, ls.L * (1.f / ls.pdf), L);
+  }
+  const float uLobe = smp.next(), ubx = smp.next(), uby = smp.next();
+  const BSDFSampleT<float> bs = m.Sample(it.geom.onb.WorldToLocal(wo), uLobe, ubx, uby);
+  const Ray r2{it.geom.p, it.geom.onb.LocalToWorld(bs.wi)};
+  float t2 = kInf;
+  Interaction it2;
+  if (sc.Closest(r2, &t2, &it2, wt, c) && sc.inst[it2.inst].light >= 0) {
+    Vector3 le;
+    float pdfL;
+    sc.EvalLight(r2.Origin, it2, &le, &pdfL);
+    L = Vector3::FusedMultiplyAdd(bs.eval.bsdf, le * (1.f / pdfL), L);
+  }
+  return L;
+}
+
 // ---------------------------------------------------------------- PSSMLT (PSSMLT.fs)
 // Giles' single-precision erfinv as the reference evaluates it (PSSMLT.fs:69-94)
 float ErfInv(float x) {
@@ -1272,6 +1316,35 @@ int or_trace(const or_scene* os, const bn_ray* rays, int64_t n, uint32_t flags, 
   return 0;
 }
 
+// Film.PostProcess (Base/Film.fs:21-30) and the Rgba32(Vector3) packing of Film.Save (:55-66):
+// ImageSharp 3.1.6 (a NuGet dependency, not vendored) packs each component as
+// (byte)clamp(v * 255 + 0.5, 0, 255), and .NET converts a NaN to 0.  Vector3.Clamp is
+// Min(Max(x, 0), 1), whose Math semantics keep a NaN.
+int or_tonemap(const float* rgb, int64_t n, int32_t tone_mapping, uint8_t* rgba) {
+  auto clamp01 = [](float x) { return x != x ? x : MathMin(MathMax(x, 0.f), 1.f); };
+  auto pack = [](float v) -> uint8_t {
+    const float w = v * 255.f + 0.5f;
+    if (w != w) return 0;
+    return static_cast<uint8_t>(static_cast<int>(std::min(std::max(w, 0.f), 255.f)));
+  };
+  for (int64_t i = 0; i < n; ++i) {
+    Vector3 x(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+    if (tone_mapping == BN_TONE_ACES) {
+      x = x * (2.51f * x + Vector3(0.03f)) / (x * (2.43f * x + Vector3(0.59f)) + Vector3(0.14f));
+    } else if (tone_mapping == BN_TONE_GAMMA) {
+      const float gamma = 1.f / 2.2f;
+      x = Vector3(std::pow(x.X, gamma), std::pow(x.Y, gamma), std::pow(x.Z, gamma));
+    } else if (tone_mapping != BN_TONE_IDENTITY) {
+      return 1;
+    }
+    rgba[4 * i] = pack(clamp01(x.X));
+    rgba[4 * i + 1] = pack(clamp01(x.Y));
+    rgba[4 * i + 2] = pack(clamp01(x.Z));
+    rgba[4 * i + 3] = 255;
+  }
+  return 0;
+}
+
 int or_sampler_stream(const uint32_t* seeds, int64_t n, int32_t draws, float* out) {
   for (int64_t i = 0; i < n; ++i) {
     Sampler s = Sampler::Three(seeds[3 * i], seeds[3 * i + 1], seeds[3 * i + 2]);
@@ -1316,7 +1389,8 @@ int or_bsdf(const bn_material_desc* md, const bn_bsdf_query* q, int64_t n, int s
   return 0;
 }
 
-// ProgressiveIntegrator.Render / RenderTile (Base/Integrator.fs:22-55) with PathTracingIntegrator:
+// ProgressiveIntegrator.Render / RenderTile (Base/Integrator.fs:22-55) with PathTracingIntegrator
+// (or the Normal / Direct integrator, by d->integrator):
 // 16x16 tiles over `threads` workers; only tiles intersecting the crop [x0,x1) x [y0,y1) render.
 // out: W*H*3 floats in Film.Pixels order (row-flipped); pixels outside the crop are left as is.
 int or_render_pt(const or_scene* os, const bn_render_desc* d, const bn_view* view, int32_t x0, int32_t y0, int32_t x1,
@@ -1346,7 +1420,10 @@ int or_render_pt(const or_scene* os, const bn_render_desc* d, const bn_view* vie
             const float upx = smp.next(), upy = smp.next();
             const float ulx = smp.next(), uly = smp.next();
             const Ray ray = cam.Generate(x, y, upx, upy, ulx, uly);
-            const Vector3 L = Li<false>(sc, ray, smp, d->max_depth, d->rr_depth, wt, &c) * (1.f / 1.f);
+            Vector3 L;
+            if (d->integrator == BN_INTEGRATOR_NORMAL) L = LiNormal(sc, ray, wt, &c);
+            else if (d->integrator == BN_INTEGRATOR_DIRECT) L = LiDirect(sc, ray, smp, wt, &c);
+            else L = Li<false>(sc, ray, smp, d->max_depth, d->rr_depth, wt, &c);
             acc = Vector3::FusedMultiplyAdd(Vector3(invSpp), L, acc);
           }
           const size_t idx = static_cast<size_t>(H - y - 1) * W + x;

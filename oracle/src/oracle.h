@@ -17,6 +17,7 @@ int or_scene_blas(const or_scene* s, int32_t mesh, bn_bvh_node* nodes, int32_t* 
 int or_bvh_build(const float* bounds, int32_t n, bn_bvh_node* nodes, int32_t* n_nodes, int32_t* perm);
 int or_trace(const or_scene* s, const bn_ray* rays, int64_t n, uint32_t flags, bn_hit* hits, uint64_t* counts);
 int or_sampler_stream(const uint32_t* seeds, int64_t n, int32_t draws, float* out);
+int or_tonemap(const float* rgb, int64_t n, int32_t tone_mapping, uint8_t* rgba);
 uint32_t or_xxhash32_two(uint32_t x, uint32_t y);
 uint32_t or_xxhash32_three(uint32_t x, uint32_t y, uint32_t z);
 int or_bsdf(const bn_material_desc* materials, const bn_bsdf_query* q, int64_t n, int sample, int use_double,

@@ -297,3 +297,74 @@ def test_library_exports_every_declared_symbol():
     assert not missing, f"declared but not exported: {missing}"
     assert declared <= set(capi.SIGNATURES), "every declared entry point has a ctypes signature"
     assert lib.bn_version().decode().startswith("barnacle-gb300")
+
+
+# ------------------------------------------------------------------ film output and integrators
+def test_json_loader_integrators_and_tone_mapping(tmp_path):
+    base = {"nodes": [{"instances": [0], "children": [1]}, {"has-camera": True}],
+            "instances": [{"primitive": 0, "light": 0}],
+            "primitives": [{"type": "sphere", "radius": 1.0}],
+            "lights": [{"type": "diffuse", "emission": [1, 1, 1]}],
+            "camera": {"type": "pinhole"}}
+    want = {"normal": capi.BN_INTEGRATOR_NORMAL, "direct": capi.BN_INTEGRATOR_DIRECT,
+            "path-tracing": capi.BN_INTEGRATOR_PATH}
+    tones = {"aces": capi.BN_TONE_ACES, "gamma": capi.BN_TONE_GAMMA, "identity": capi.BN_TONE_IDENTITY}
+    for (itype, ival), (tname, tval) in zip(want.items(), tones.items()):
+        p = tmp_path / f"{itype}.json"
+        p.write_text(json.dumps({**base, "integrator": {"type": itype, "spp": 3},
+                                 "film": {"width": 4, "height": 2, "tone-mapping": tname}}))
+        b = Bundle.load_json(str(p))
+        assert b.render.integrator == ival and b.render.spp == 3 and b.tone_mapping == tval
+    p = tmp_path / "bad.json"
+    p.write_text(json.dumps({**base, "integrator": {"type": "normal"},
+                             "film": {"width": 4, "height": 2, "tone-mapping": "filmic"}}))
+    with pytest.raises(BarnacleError, match="Unknown tone mapping type"):
+        Bundle.load_json(str(p))
+    assert Bundle.generate("cornell").tone_mapping == capi.BN_TONE_ACES
+
+
+def test_oracle_tonemap_against_float32_formulas():
+    """Film.PostProcess restated independently in numpy float32 (ACES fit, clamp) and the Rgba32
+    packing floor(255 v + 0.5)."""
+    from oracle import pyoracle
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(0, 4, (4000, 3)), [[0, 0.5, 1], [2, 1e-8, 100]]]).astype(np.float32)
+    f = np.float32
+    aces = (x * (f(2.51) * x + f(0.03))) / (x * (f(2.43) * x + f(0.59)) + f(0.14))
+    for tm, y in ((capi.BN_TONE_IDENTITY, x), (capi.BN_TONE_ACES, aces)):
+        y = np.clip(y, f(0), f(1))
+        want = np.floor(y * f(255) + f(0.5)).astype(np.uint8)
+        got = pyoracle.tonemap(x, tm)
+        assert np.array_equal(got[:, :3], want) and (got[:, 3] == 255).all()
+    g = pyoracle.tonemap(x, capi.BN_TONE_GAMMA)[:, :3].astype(int)
+    ref = np.floor(np.clip(x.astype(np.float64) ** (1 / 2.2), 0, 1) * 255 + 0.5)
+    assert np.abs(g - ref).max() <= 1
+    # NaN packs to 0; the ACES fit maps -1 to 2.48 / 1.98 > 1 and 7 near 1
+    nan = pyoracle.tonemap(np.array([[np.nan, -1, 7]], np.float32), capi.BN_TONE_ACES)
+    assert nan[0].tolist() == [0, 255, 255, 255]
+    assert pyoracle.tonemap(np.array([[np.nan, -1, 0.25]], np.float32), capi.BN_TONE_IDENTITY)[0].tolist() == \
+        [0, 0, 64, 255]
+
+
+def test_png_writer_round_trip(tmp_path):
+    import struct
+    import zlib
+    from barnacle_gb300 import write_png
+    rng = np.random.default_rng(0)
+    for h, w in ((1, 1), (7, 13), (300, 200)):  # 300 x 801 bytes: several stored blocks
+        img = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+        p = tmp_path / f"i{h}.png"
+        write_png(p, img)
+        data = p.read_bytes()
+        assert data[:8] == b"\x89PNG\r\n\x1a\n"
+        pos, chunks = 8, {}
+        while pos < len(data):
+            n = struct.unpack(">I", data[pos:pos + 4])[0]
+            typ = data[pos + 4:pos + 8]
+            body = data[pos + 8:pos + 8 + n]
+            assert struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(typ + body)
+            chunks[typ] = chunks.get(typ, b"") + body
+            pos += 12 + n
+        assert struct.unpack(">IIBBBBB", chunks[b"IHDR"]) == (w, h, 8, 6, 0, 0, 0)
+        raw = np.frombuffer(zlib.decompress(chunks[b"IDAT"]), np.uint8).reshape(h, 1 + 4 * w)
+        assert (raw[:, 0] == 0).all() and np.array_equal(raw[:, 1:].reshape(h, w, 4), img)
