@@ -175,6 +175,16 @@ class Context:
             off += n
         return imgs
 
+    def bvh_build(self, bounds: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """BVHNode.Build on this context's GPU: the same (nodes, permutation) as bvh_build."""
+        b = np.ascontiguousarray(bounds, np.float32).reshape(-1, 6)
+        n = len(b)
+        nodes = np.zeros(max(2 * n, 1), capi.NODE_DTYPE)
+        nn = C.c_int32()
+        perm = np.zeros(max(n, 1), np.int32)
+        self._check(self.lib.bn_bvh_build_device(self._h, ptr(b), n, ptr(nodes), C.byref(nn), ptr(perm)))
+        return nodes[: nn.value], perm[:n]
+
     def film_download(self, out: np.ndarray) -> None:
         self._check(self.lib.bn_film_download(self._h, ptr(out), out.size))
 

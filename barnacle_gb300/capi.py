@@ -26,6 +26,7 @@ BN_MAT_LAMBERTIAN, BN_MAT_MIRROR, BN_MAT_DIELECTRIC, BN_MAT_PBR = 0, 1, 2, 3
 BN_CAM_PINHOLE, BN_CAM_THIN_LENS = 0, 1
 BN_LIGHTS_UNIFORM, BN_LIGHTS_ALIAS_TRIANGLES = 0, 1
 BN_BVH_AUTO, BN_BVH_BINARY, BN_BVH_WIDE = 0, 2, 4
+BN_BUILDER_AUTO, BN_BUILDER_HOST, BN_BUILDER_DEVICE = 0, 1, 2
 BN_TONE_IDENTITY, BN_TONE_ACES, BN_TONE_GAMMA = 0, 1, 2
 BN_TRACE_CLOSEST, BN_TRACE_ANY, BN_TRACE_WATERTIGHT, BN_TRACE_COUNT = 0x0, 0x1, 0x2, 0x4
 BN_INTEGRATOR_PATH, BN_INTEGRATOR_PSSMLT, BN_INTEGRATOR_NORMAL, BN_INTEGRATOR_DIRECT = 0, 1, 2, 3
@@ -70,7 +71,7 @@ class bn_scene_desc(C.Structure):
                 ("instances", C.POINTER(bn_instance_desc)), ("n_instances", C.c_int32),
                 ("materials", C.POINTER(bn_material_desc)), ("n_materials", C.c_int32),
                 ("lights", C.POINTER(bn_light_desc)), ("n_lights", C.c_int32),
-                ("light_sampler", C.c_int32), ("bvh_width", C.c_int32)]
+                ("light_sampler", C.c_int32), ("bvh_width", C.c_int32), ("bvh_builder", C.c_int32)]
 
 
 class bn_ray(C.Structure):
@@ -170,6 +171,7 @@ SIGNATURES = {
     "bn_forward": (C.c_int, [P, C.POINTER(bn_adjoint_desc), P, P, P]),
     "bn_backward": (C.c_int, [P, C.POINTER(bn_adjoint_desc), P, P, P, P, P]),
     "bn_bvh_build": (C.c_int, [P, C.c_int32, P, P, P]),
+    "bn_bvh_build_device": (C.c_int, [P, P, C.c_int32, P, P, P]),
     "bn_mat4_invert": (C.c_int, [P, P]),
     "bn_bundle_generate": (C.c_int, [C.c_char_p, C.c_uint32, C.POINTER(P)]),
     "bn_bundle_load_json": (C.c_int, [C.c_char_p, C.POINTER(P)]),

@@ -78,5 +78,8 @@ namespace bnc {
 bn::DevView make_dev_view(const bn_view& v, long long pixel_offset, long long path_offset);
 int check_device_error(bn_context* ctx);
 int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views);
+// BVHNode.Build on the GPU (bvh_gpu.cu): the host builder's nodes and permutation
+int gpu_bvh_build(bn_context* ctx, const float* bounds, int32_t n, std::vector<bn_bvh_node>* nodes,
+                  std::vector<int32_t>* perm, int small);
 int render_pssmlt(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views);
 }  // namespace bnc

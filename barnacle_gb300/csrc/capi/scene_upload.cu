@@ -1,7 +1,8 @@
 // bn_scene_upload: the host preparation of the render call, then one upload.
 //
 //  1. BLAS per mesh over the triangle AABBs (MeshPrimitive.BVHNodes, Mesh.fs:159-169), which
-//     permutes the mesh's triangles in place; triangles are stored in that order.
+//     permutes the mesh's triangles in place; triangles are stored in that order.  Built on the
+//     GPU (bvh_gpu.cu) or the host (bvh_build.cpp), which give the same trees.
 //  2. the reference AliasTable of each mesh over triangle areas in permuted order
 //     (Mesh.fs:181-186, Util/AliasTable.fs:14-27): entry pdf = area / (sequential float sum).
 //  3. instance world bounds = AxisAlignedBoundingBox.Transform(BLAS root bounds, ObjectToWorld)
@@ -212,6 +213,11 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
       return ctx->fail(BN_ERR_INVALID_ARG, "material " + std::to_string(i) + ": unknown type");
 
   // ---- 1+2: BLAS per mesh, permuted triangles, reference alias pdf
+  if (d->bvh_builder != BN_BUILDER_AUTO && d->bvh_builder != BN_BUILDER_HOST && d->bvh_builder != BN_BUILDER_DEVICE)
+    return ctx->fail(BN_ERR_INVALID_ARG, "bvh_builder must be 0 (auto), 1 (host) or 2 (device)");
+  auto on_device = [&](int n) {
+    return d->bvh_builder == BN_BUILDER_DEVICE || (d->bvh_builder == BN_BUILDER_AUTO && n >= 16384);
+  };
   std::vector<MeshPrep> mp(d->n_meshes);
   std::vector<float4> tris;
   std::vector<float> tri_pdf;
@@ -226,8 +232,12 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
       float* b = &boxes[6 * static_cast<size_t>(t)];
       b[0] = lo.x; b[1] = lo.y; b[2] = lo.z; b[3] = hi.x; b[4] = hi.y; b[5] = hi.z;
     }
-    if (!bnh::bvh_build(boxes.data(), m.n_triangles, &mp[i].nodes, &mp[i].perm))
+    if (on_device(m.n_triangles)) {
+      const int rc = bnc::gpu_bvh_build(ctx, boxes.data(), m.n_triangles, &mp[i].nodes, &mp[i].perm, 256);
+      if (rc) return rc;
+    } else if (!bnh::bvh_build(boxes.data(), m.n_triangles, &mp[i].nodes, &mp[i].perm)) {
       return ctx->fail(BN_ERR_UNSUPPORTED, "mesh " + std::to_string(i) + ": BVH leaf larger than 127 triangles");
+    }
     mp[i].tri_base = static_cast<int>(tris.size() / 3);
     mp[i].node_base = static_cast<int>(blas_nodes);
     blas_nodes += mp[i].nodes.size();
@@ -282,8 +292,12 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   // ---- 4: TLAS
   std::vector<bn_bvh_node> tlas;
   std::vector<int32_t> order;
-  if (!bnh::bvh_build(ibox.data(), ni, &tlas, &order))
+  if (on_device(ni)) {
+    const int rc = bnc::gpu_bvh_build(ctx, ibox.data(), ni, &tlas, &order, 256);
+    if (rc) return rc;
+  } else if (!bnh::bvh_build(ibox.data(), ni, &tlas, &order)) {
     return ctx->fail(BN_ERR_UNSUPPORTED, "TLAS leaf larger than 127 instances");
+  }
   const int n_tlas = static_cast<int>(tlas.size());
   std::vector<float4> nodes(2 * (tlas.size() + blas_nodes));
   for (size_t k = 0; k < tlas.size(); ++k) put_node(&nodes[2 * k], tlas[k]);

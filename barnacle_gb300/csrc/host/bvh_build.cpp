@@ -4,6 +4,7 @@
 //   * 12 bins, leaves of <= 4 items, depth cut at 64            (Util/BVH.fs:99-107)
 //   * split axis = longest centroid-bounds axis; median split when its extent is 0 (:147-156)
 //   * bin = min(11, int(12 * (c - cmin) / extent))                                  (:163-169)
+//     with .NET 9's saturating conversion (NaN -> 0), which infinite boxes reach
 //   * cost[i] = SAH(bins 0..i) + SAH(bins i+1..11) + n * SA(centroid bounds)        (:179-203)
 //   * unstable partition: items in bins > best fill from the end, the rest from the front,
 //     both read from a copy of the subrange                                          (:205-217)
@@ -39,6 +40,13 @@ static inline V3 centroid(const Box& b) { return 0.5f * (b.lo + b.hi); }
 static inline float surface_area(const Box& b) {
   V3 d = b.hi - b.lo;
   return 2.f * ((d.x * d.y + d.y * d.z) + d.z * d.x);
+}
+// float -> int32 as .NET 9 converts: truncation, saturated at the int range, NaN -> 0
+static inline int saturating_int(float f) {
+  if (f != f) return 0;
+  if (f >= 2147483647.f) return 2147483647;
+  if (f <= -2147483648.f) return -2147483647 - 1;
+  return static_cast<int>(f);
 }
 static inline int split_axis(const Box& b) {
   V3 d = b.hi - b.lo;
@@ -90,7 +98,8 @@ struct Builder {
     } else {
       const float cmin = comp(cb.lo, axis);
       auto bin_of = [&](const Box& b) {
-        int k = static_cast<int>((static_cast<float>(kBins) * (comp(centroid(b), axis) - cmin)) / extent);
+        // .NET's saturating float -> int conversion: a NaN (inf - inf with infinite boxes) is 0
+        int k = saturating_int((static_cast<float>(kBins) * (comp(centroid(b), axis) - cmin)) / extent);
         return k < kBins - 1 ? k : kBins - 1;
       };
       Box bin_box[kBins];

@@ -62,6 +62,9 @@ enum bn_light_sampler_type {
  * for scenes of at least 1,024 BVH nodes, where halving the dependent node loads pays for the
  * wider tests.  Visit counting (BN_TRACE_COUNT, BN_RENDER_COUNT) always walks the binary tree. */
 enum bn_bvh_width { BN_BVH_AUTO = 0, BN_BVH_BINARY = 2, BN_BVH_WIDE = 4 };
+/* Where bn_scene_upload builds the BLASes and the TLAS; both builders give the same trees
+ * (BVHNode.Build, Util/BVH.fs:239-247).  AUTO builds on the GPU from 16,384 boxes on. */
+enum bn_bvh_builder { BN_BUILDER_AUTO = 0, BN_BUILDER_HOST = 1, BN_BUILDER_DEVICE = 2 };
 
 /* MeshPrimitive(vertices, indices) (Extensions/Primitive/Mesh.fs:120) */
 typedef struct bn_mesh_desc {
@@ -123,6 +126,7 @@ typedef struct bn_scene_desc {
   const bn_light_desc* lights;         int32_t n_lights;
   int32_t light_sampler;               /* bn_light_sampler_type */
   int32_t bvh_width;                   /* bn_bvh_width (0 = auto) */
+  int32_t bvh_builder;                 /* bn_bvh_builder (0 = auto) */
 } bn_scene_desc;
 
 /* ---- ray queries (Extensions/Aggregate/BVH.fs:11-58) ----------------------------------- */
@@ -331,6 +335,11 @@ typedef struct bn_bvh_node {
  * in-place permutation. */
 int bn_bvh_build(const float* bounds, int32_t n, bn_bvh_node* nodes_out, int32_t* n_nodes_out,
                  int32_t* perm_out);
+/* The same build on the GPU of ctx, with the same nodes and permutation: node ranges above 256
+ * items are split level by level on the device, smaller ones by one device thread each.  Boxes
+ * with a NaN coordinate are built by the host builder. */
+int bn_bvh_build_device(bn_context* ctx, const float* bounds, int32_t n, bn_bvh_node* nodes_out,
+                        int32_t* n_nodes_out, int32_t* perm_out);
 /* Matrix4x4.Invert restated (used by Node.Traverse -> UpdateTransform) */
 int bn_mat4_invert(const float m[16], float out[16]);
 

@@ -160,7 +160,9 @@ std::unique_ptr<Tree> TreeBuild(std::vector<BuildItem>& instances, int first, in
   int binC[12];
   for (int i = 0; i < 12; ++i) { binB[i] = AABB::Default(); binC[i] = 0; }
   auto findBin = [&](const BuildItem& it) {
-    const int b = static_cast<int>((12.f * (it.bounds.Centroid()[axis] - cb.pMin[axis])) / extent);
+    // int(...) converts as .NET 9 does: truncation, saturated, NaN -> 0 (infinite boxes give NaN)
+    const float f = (12.f * (it.bounds.Centroid()[axis] - cb.pMin[axis])) / extent;
+    const int b = f != f ? 0 : (f >= 2147483647.f ? 2147483647 : static_cast<int>(f));
     return std::min(11, b);
   };
   for (int i = first; i < last; ++i) {
