@@ -95,6 +95,20 @@ static inline V3 translation(const M4& M) { return {M.m[12], M.m[13], M.m[14]}; 
 // 1/det.  Returns false (and a NaN matrix, as System.Numerics does) when |det| < eps.
 bool m4_invert(const M4& in, M4* out);
 
+// KeyFrame.Interpolate (Base/Scene.fs:13-20) for a render time between two keyframes: ratio =
+// (t - ta) / (tb - ta); Matrix4x4.Decompose of both matrices into (scale, rotation, translation);
+// Vector3.Lerp of scales and translations, Quaternion.Slerp of rotations; then
+// Transform.Compose(scale, rotation, translation) (Util/Transform.fs:6-9), which builds
+// CreateTranslation(scale) * CreateFromQuaternion(rotation) * CreateScale(translation) — the
+// reference swaps scale and translation there, and that is kept.  The System.Numerics routines
+// (.NET 9 BCL, not vendored) are restated from their published source.
+M4 keyframe_interpolate(float ta, const M4& a, float tb, const M4& b, float t);
+// Matrix4x4.Decompose: false for a matrix that is not scale-rotation-translation
+bool m4_decompose(const M4& m, V3* scale, float rotation[4], V3* translation);
+M4 m4_from_quaternion(const float q[4]);
+void quat_slerp(const float a[4], const float b[4], float t, float out[4]);
+float m4_determinant(const M4& m);
+
 // Deterministic sine/cosine in double precision (range reduction + Taylor series).  The
 // procedural scene generators use it so that the generated geometry has the same bits on
 // every host, whatever its libm.

@@ -5,8 +5,11 @@
 // Schema facts kept from the reference:
 //  * keyframe matrix = CreateScale * (RotX * RotY * RotZ) * CreateTranslation, rotation values
 //    in RADIANS, passed straight to CreateRotationX/Y/Z (Loader.fs:24-45)
-//  * Transform.Eval(t): the last keyframe with time <= t; before the first keyframe, the first
-//    (Scene.fs:27-36).  Interpolation between two keyframes is not supported by this loader.
+//  * Transform.Eval(t): the last keyframe with time <= t; before the first keyframe, the first;
+//    between two keyframes KeyFrame.Interpolate (Scene.fs:13-36), with the reference's
+//    Transform.Compose that swaps scale and translation (keyframe_interpolate, host_math.cpp).
+//    Scene.Render is called with t = 0 (Program.fs:27), so interpolation happens for
+//    keyframes on both sides of time 0.
 //  * node world matrix = Eval(t) * parent (local . parent, row vectors) (Scene.fs:44)
 //  * an instance listed under several nodes appears once per listing, all with the transform
 //    of the last traversal (PrimitiveInstance is one mutable object, Primitive.fs:131-138)
@@ -344,7 +347,7 @@ bool load_json_bundle(const std::string& path, bn_scene_bundle* b, std::string* 
         if (ks[k].time <= t_render) { prev = k; break; }
       if (prev < 0) local = ks[0].m;
       else if (prev == static_cast<int>(ks.size()) - 1) local = ks[prev].m;
-      else { *err = "keyframe interpolation is not supported (render time between two keyframes)"; return false; }
+      else local = keyframe_interpolate(ks[prev].time, ks[prev].m, ks[prev + 1].time, ks[prev + 1].m, t_render);
     }
     const M4 world = m4_mul(local, parent);
     if (nd.camera) camera_xf = world;

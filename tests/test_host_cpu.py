@@ -368,3 +368,40 @@ def test_png_writer_round_trip(tmp_path):
         assert struct.unpack(">IIBBBBB", chunks[b"IHDR"]) == (w, h, 8, 6, 0, 0, 0)
         raw = np.frombuffer(zlib.decompress(chunks[b"IDAT"]), np.uint8).reshape(h, 1 + 4 * w)
         assert (raw[:, 0] == 0).all() and np.array_equal(raw[:, 1:].reshape(h, w, 4), img)
+
+
+def test_json_loader_interpolates_keyframes_around_time_zero(tmp_path):
+    """Scene.Render renders t = 0 (Program.fs:27); a transform with keyframes at t = -1 and t = 1
+    is interpolated (Scene.fs:13-20): scales and translations lerp to their midpoints, and
+    Transform.Compose (Util/Transform.fs:6-9) then builds CreateTranslation(scale) *
+    CreateFromQuaternion(rotation) * CreateScale(translation) — scale and translation swapped, as
+    in the reference."""
+    def scene(keys):
+        return {"transforms": [{"keyframes": keys}],
+                "nodes": [{"instances": [0], "transform": 0, "children": [1]}, {"has-camera": True}],
+                "instances": [{"primitive": 0, "light": 0}],
+                "primitives": [{"type": "sphere", "radius": 1.0}],
+                "lights": [{"type": "diffuse", "emission": [1, 1, 1]}],
+                "integrator": {"type": "path-tracing"}, "camera": {"type": "pinhole"},
+                "film": {"width": 4, "height": 4, "tone-mapping": "aces"}}
+    p = tmp_path / "kf.json"
+    p.write_text(json.dumps(scene([
+        {"time": -1, "scale": [1, 1, 1], "translation": [0, 0, 0]},
+        {"time": 1, "scale": [3, 3, 3], "translation": [2, 4, 6]}])))
+    m = np.array(Bundle.load_json(str(p)).scene.contents.instances[0].object_to_world, np.float32).reshape(4, 4)
+    want = np.diag([1, 2, 3, 1]).astype(np.float32)   # CreateScale(translation (1, 2, 3))
+    want[3, :3] = [2 * 1, 2 * 2, 2 * 3]                 # CreateTranslation(scale (2, 2, 2)) * that
+    np.testing.assert_allclose(m, want, atol=1e-6)
+    # a rotation interpolated by Slerp: 0 and pi/2 about y give pi/4
+    p.write_text(json.dumps(scene([
+        {"time": -1, "rotation": [0, 0, 0], "translation": [1, 1, 1]},
+        {"time": 1, "rotation": [0, np.pi / 2, 0], "translation": [1, 1, 1]}])))
+    m = np.array(Bundle.load_json(str(p)).scene.contents.instances[0].object_to_world, np.float32).reshape(4, 4)
+    c = np.cos(np.pi / 4)
+    rot = np.array([[c, 0, -c], [0, 1, 0], [c, 0, c]], np.float32)  # CreateRotationY(pi/4), row vectors
+    np.testing.assert_allclose(m[:3, :3], rot, atol=1e-5)  # CreateScale(translation (1, 1, 1)) = I
+    np.testing.assert_allclose(m[3, :3], rot.sum(0), atol=1e-5)  # translation row (1, 1, 1) * R
+    # at or after the last keyframe, and before the first, no interpolation
+    p.write_text(json.dumps(scene([{"time": 0, "translation": [5, 0, 0]}, {"time": 2, "translation": [9, 0, 0]}])))
+    m = np.array(Bundle.load_json(str(p)).scene.contents.instances[0].object_to_world, np.float32).reshape(4, 4)
+    assert list(m[3, :3]) == [5, 0, 0]
