@@ -371,9 +371,12 @@ def main():
     dom_launch_s = dom_ms / 1000.0 / args.steps
     achieved = alg_bytes / dom_launch_s / 1e9
     traffic = None
-    prof = ROOT / "profiles" / f"traffic_{args.mode}_{args.workload}.json"
-    if prof.exists():
-        traffic = json.loads(prof.read_text()).get("bytes_per_launch")
+    prof = ROOT / "profiles" / f"traffic_{args.mode}_{args.workload}.md"
+    if prof.exists():  # an ncu summary with a "bytes_per_launch: N" line
+        for line in prof.read_text().splitlines():
+            if line.startswith("bytes_per_launch:"):
+                # measured at the default 4 spp per step; other step sizes report none
+                traffic = int(line.split(":")[1]) if args.spp_per_step == 4 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
