@@ -274,77 +274,77 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     // one triangle of a BLAS leaf: its AABB pre-test (Mesh.fs:204,231), then the triangle test
 #pragma unroll 1
     while (tr.ti < tr.ti_end) {
-    const int j = tr.ti++;
-    const float4* tp = s.tris + 3 * (tr.tri_base + j);
-    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-    if (kCount) cnt->tris++;
-    const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
-    const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
-    if (box_hit(lo, hi, tr.orr, tr.oinv, tr.t)) {
-      float tt, uu, vv;
-      const bool h = kWT ? tri_wt(p0, p1, p2, tr.orr, tr.wt, tr.t, &tt, &uu, &vv)
-                         : tri_mt(p0, p1, p2, tr.orr, tr.t, &tt, &uu, &vv);
-      if (h) {
-        tr.found = true;
-        if (any) {
-          tr.mode = kTravDone;
-          return true;
+      const int j = tr.ti++;
+      const float4* tp = s.tris + 3 * (tr.tri_base + j);
+      const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+      if (kCount) cnt->tris++;
+      const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
+      const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
+      if (box_hit(lo, hi, tr.orr, tr.oinv, tr.t)) {
+        float tt, uu, vv;
+        const bool h = kWT ? tri_wt(p0, p1, p2, tr.orr, tr.wt, tr.t, &tt, &uu, &vv)
+                           : tri_mt(p0, p1, p2, tr.orr, tr.t, &tt, &uu, &vv);
+        if (h) {
+          tr.found = true;
+          if (any) {
+            tr.mode = kTravDone;
+            return true;
+          }
+          tr.t = tt;
+          tr.hit.inst = tr.inst; tr.hit.tri = j; tr.hit.t = tt; tr.hit.u = uu; tr.hit.v = vv; tr.hit.sphere_root = 0;
         }
-        tr.t = tt;
-        tr.hit.inst = tr.inst; tr.hit.tri = j; tr.hit.t = tt; tr.hit.u = uu; tr.hit.v = vv; tr.hit.sphere_root = 0;
       }
-    }
-    if (kFine) break;
+      if (kFine) break;
     }
     pop = tr.ti >= tr.ti_end;
   } else if (tr.mode == kTravInst) {
     // one instance of a TLAS leaf (PrimitiveInstance.Intersect, Primitive.fs:111-129)
     bool entered = false;
     if (tr.ii < tr.ii_end) {
-    const int k = tr.ii++;
-    const DevInstance* I = s.inst + k;
-    if (kCount) cnt->insts++;
-    const float4 bmin = __ldg(&I->bmin), bmax = __ldg(&I->bmax);
-    if (box_hit(xyz(bmin), xyz(bmax), tr.wr, tr.winv, tr.t)) {
-      float4 w2o[3];
-      load_xf(I->w2o, w2o);
-      tr.orr.o = xf_point(w2o, tr.wr.o);
-      tr.orr.d = xf_dir(w2o, tr.wr.d);
-      if (__ldg(&I->prim_type) == kPrimSphere) {
-        float ts;
-        const int root = sphere_hit(bmax.w, tr.orr, tr.t, &ts);
-        if (root) {
-          tr.found = true;
-          if (any) {
-            tr.mode = kTravDone;
-            return true;
+      const int k = tr.ii++;
+      const DevInstance* I = s.inst + k;
+      if (kCount) cnt->insts++;
+      const float4 bmin = __ldg(&I->bmin), bmax = __ldg(&I->bmax);
+      if (box_hit(xyz(bmin), xyz(bmax), tr.wr, tr.winv, tr.t)) {
+        float4 w2o[3];
+        load_xf(I->w2o, w2o);
+        tr.orr.o = xf_point(w2o, tr.wr.o);
+        tr.orr.d = xf_dir(w2o, tr.wr.d);
+        if (__ldg(&I->prim_type) == kPrimSphere) {
+          float ts;
+          const int root = sphere_hit(bmax.w, tr.orr, tr.t, &ts);
+          if (root) {
+            tr.found = true;
+            if (any) {
+              tr.mode = kTravDone;
+              return true;
+            }
+            tr.t = ts;
+            tr.hit.inst = k; tr.hit.tri = 0; tr.hit.sphere_root = root; tr.hit.t = ts; tr.hit.u = 0.f; tr.hit.v = 0.f;
           }
-          tr.t = ts;
-          tr.hit.inst = k; tr.hit.tri = 0; tr.hit.sphere_root = root; tr.hit.t = ts; tr.hit.u = 0.f; tr.hit.v = 0.f;
-        }
-      } else {
-        tr.oinv = inv_dir(tr.orr.d);
-        if (kWT) tr.wt = wt_setup(tr.orr.d);
-        const int base = __ldg(&I->node_base);
-        const NodeRec root = load_node(s.nodes, base);
-        if (kCount) cnt->nodes++;
-        float te;
-        if (box_hit_t(root.bmin, root.bmax, tr.orr, tr.oinv, tr.t, &te)) {
-          tr.level = 1;
-          tr.base = base;
-          tr.tri_base = __ldg(&I->tri_base);
-          tr.inst = k;
-          tr.blas_sp0 = tr.sp;
-          if (!kWide || root.leaf) {
-            trav_enter(tr, 0, root);
-          } else {
-            tr.cur = __ldg(&I->node4_root);
-            tr.mode = kTravNode;
+        } else {
+          tr.oinv = inv_dir(tr.orr.d);
+          if (kWT) tr.wt = wt_setup(tr.orr.d);
+          const int base = __ldg(&I->node_base);
+          const NodeRec root = load_node(s.nodes, base);
+          if (kCount) cnt->nodes++;
+          float te;
+          if (box_hit_t(root.bmin, root.bmax, tr.orr, tr.oinv, tr.t, &te)) {
+            tr.level = 1;
+            tr.base = base;
+            tr.tri_base = __ldg(&I->tri_base);
+            tr.inst = k;
+            tr.blas_sp0 = tr.sp;
+            if (!kWide || root.leaf) {
+              trav_enter(tr, 0, root);
+            } else {
+              tr.cur = __ldg(&I->node4_root);
+              tr.mode = kTravNode;
+            }
+            entered = true;
           }
-          entered = true;
         }
       }
-    }
     }
     pop = !entered && tr.ii >= tr.ii_end;
   }
