@@ -345,6 +345,11 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
     di.light = in.light;
     di.light_entry_base = -1;
     di.node4_root = p.type == BN_PRIM_MESH ? mp[p.mesh].node4_root : -1;
+    if (p.type == BN_PRIM_MESH) {
+      const bn_bvh_node& r = mp[p.mesh].nodes[0];
+      di.rbmin = make_float4(r.bounds_min[0], r.bounds_min[1], r.bounds_min[2], 0.f);
+      di.rbmax = make_float4(r.bounds_max[0], r.bounds_max[1], r.bounds_max[2], 0.f);
+    }
     inst_light[k] = in.light;
   }
 

@@ -304,13 +304,18 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
       const int k = tr.ii++;
       const DevInstance* I = s.inst + k;
       if (kCount) cnt->insts++;
-      const float4 bmin = __ldg(&I->bmin), bmax = __ldg(&I->bmax);
+      // the instance's first line in eight independent loads: bounds, WorldToObject, the BLAS
+      // root's box and the indices, so one memory round trip serves the whole visit
+      const float4* line = reinterpret_cast<const float4*>(I);
+      const float4 bmin = __ldg(line), bmax = __ldg(line + 1);
+      float4 w2o[3];
+      w2o[0] = __ldg(line + 2); w2o[1] = __ldg(line + 3); w2o[2] = __ldg(line + 4);
+      const float4 rlo = __ldg(line + 5), rhi = __ldg(line + 6);
+      const int4 ids = __ldg(reinterpret_cast<const int4*>(line + 7));  // prim_type, node_base, tri_base, node4_root
       if (box_hit(xyz(bmin), xyz(bmax), tr.wr, tr.winv, tr.t)) {
-        float4 w2o[3];
-        load_xf(I->w2o, w2o);
         tr.orr.o = xf_point(w2o, tr.wr.o);
         tr.orr.d = xf_dir(w2o, tr.wr.d);
-        if (__ldg(&I->prim_type) == kPrimSphere) {
+        if (ids.x == kPrimSphere) {
           float ts;
           const int root = sphere_hit(bmax.w, tr.orr, tr.t, &ts);
           if (root) {
@@ -325,23 +330,32 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
         } else {
           tr.oinv = inv_dir(tr.orr.d);
           if (kWT) tr.wt = wt_setup(tr.orr.d);
-          const int base = __ldg(&I->node_base);
-          const NodeRec root = load_node(s.nodes, base);
-          if (kCount) cnt->nodes++;
+          const int base = ids.y;
           float te;
-          if (box_hit_t(root.bmin, root.bmax, tr.orr, tr.oinv, tr.t, &te)) {
-            tr.level = 1;
-            tr.base = base;
-            tr.tri_base = __ldg(&I->tri_base);
-            tr.inst = k;
-            tr.blas_sp0 = tr.sp;
-            if (!kWide || root.leaf) {
-              trav_enter(tr, 0, root);
-            } else {
-              tr.cur = __ldg(&I->node4_root);
+          if (kWide && ids.w >= 0) {
+            // the root's box from the instance line, its record next (the root is interior)
+            if (box_hit_t(xyz(rlo), xyz(rhi), tr.orr, tr.oinv, tr.t, &te)) {
+              tr.level = 1;
+              tr.base = base;
+              tr.tri_base = ids.z;
+              tr.inst = k;
+              tr.blas_sp0 = tr.sp;
+              tr.cur = ids.w;
               tr.mode = kTravNode;
+              entered = true;
             }
-            entered = true;
+          } else {
+            const NodeRec root = load_node(s.nodes, base);
+            if (kCount) cnt->nodes++;
+            if (box_hit_t(root.bmin, root.bmax, tr.orr, tr.oinv, tr.t, &te)) {
+              tr.level = 1;
+              tr.base = base;
+              tr.tri_base = ids.z;
+              tr.inst = k;
+              tr.blas_sp0 = tr.sp;
+              trav_enter(tr, 0, root);
+              entered = true;
+            }
           }
         }
       }

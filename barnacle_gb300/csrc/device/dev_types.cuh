@@ -34,21 +34,25 @@ namespace bn {
 enum : int { kPrimMesh = 0, kPrimSphere = 1 };
 enum : int { kMatLambertian = 0, kMatMirror = 1, kMatDielectric = 2, kMatPBR = 3 };
 
-struct alignas(16) DevInstance {
+// Two 128-byte lines: the first holds everything a walk reads when it visits the instance (read
+// with eight independent 16-byte loads), the second what shading reads.
+struct alignas(128) DevInstance {
   float4 bmin;      // world AABB min, .w unused
   float4 bmax;      // world AABB max, .w = sphere radius
   float4 w2o[3];    // w2o[r] = (M1r, M2r, M3r, M4r) of WorldToObject: x'_r = ((x*M1r + y*M2r) + z*M3r) + M4r
-  float4 o2w[3];    // same for ObjectToWorld
+  float4 rbmin;     // the BLAS root's box (object space) min, .w unused
+  float4 rbmax;     // the BLAS root's box max, .w unused
   int prim_type;    // kPrimMesh / kPrimSphere
   int node_base;    // BLAS root in nodes[]
   int tri_base;     // first triangle of the mesh in tris[]
+  int node4_root;   // nodes4 record of the BLAS root; -1: binary scene, leaf root or sphere
+  float4 o2w[3];    // as w2o for ObjectToWorld
   int n_tris;
   int material;     // -1 = no material (a light only; the path ends there)
   int light;        // -1 = not emissive
   int light_entry_base;  // alias-triangles: entry index of triangle 0 of this instance, -1 if none
-  int node4_root;   // nodes4 record of the BLAS root; -1: binary scene, leaf root or sphere
 };
-static_assert(sizeof(DevInstance) == 160, "DevInstance layout");
+static_assert(sizeof(DevInstance) == 256, "DevInstance layout");
 
 struct alignas(16) DevMaterial {
   int type;
