@@ -95,6 +95,9 @@ int render_megakernel(bn_context* ctx, const bn_render_desc* d, const std::vecto
   p.rr_depth = d->rr_depth;
   p.frame_id = d->frame_id;
   p.integrator = d->integrator;
+  p.simple = ctx->scene_simple;
+  for (const bn::DevView& v : views)
+    if (v.cam_type == BN_CAM_THIN_LENS && v.aperture > 0.f) p.simple = false;
   p.watertight = d->flags & BN_RENDER_WATERTIGHT;
   p.count = count;
   p.partial = ctx->partial.as<float4>();

@@ -46,6 +46,7 @@ struct bn_context {
   std::vector<int32_t> host_inst_light;  // per TLAS instance: light index
   int n_lights = 0;
   float scene_lo[3] = {0.f, 0.f, 0.f}, scene_hi[3] = {0.f, 0.f, 0.f};  // TLAS root box
+  bool scene_simple = false;  // Lambertian materials, triangle meshes, the uniform light sampler
 
   // queries
   DevBuf q_in, q_out;

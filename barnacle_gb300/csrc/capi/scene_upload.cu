@@ -457,6 +457,10 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
     ctx->scene_lo[a] = tlas[0].bounds_min[a];
     ctx->scene_hi[a] = tlas[0].bounds_max[a];
   }
+  bool simple = d->light_sampler == BN_LIGHTS_UNIFORM;
+  for (int i = 0; i < d->n_materials; ++i) simple = simple && d->materials[i].type == BN_MAT_LAMBERTIAN;
+  for (int k = 0; k < ni; ++k) simple = simple && dinst[k].prim_type == bn::kPrimMesh;
+  ctx->scene_simple = simple;
   ctx->inst_order.assign(order.begin(), order.end());
   ctx->host_mats = mats;
   ctx->host_inst_light = inst_light;

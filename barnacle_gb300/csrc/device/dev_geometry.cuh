@@ -258,6 +258,7 @@ struct Interaction {
   int tri;
 };
 
+template <bool kSimple = false>  // triangle meshes only
 __device__ __forceinline__ Interaction make_interaction(const DevScene& s, const Ray& ray, const HitRec& h) {
   const DevInstance* I = s.inst + h.inst;
   float4 w2o[3], o2w[3];
@@ -271,7 +272,7 @@ __device__ __forceinline__ Interaction make_interaction(const DevScene& s, const
   it.tri = h.tri;
   V3 p_obj;
   Onb f_obj;
-  if (__ldg(&I->prim_type) == kPrimSphere) {
+  if (!kSimple && __ldg(&I->prim_type) == kPrimSphere) {
     p_obj = point_at(oray, h.t);
     V3 n = normalize(p_obj);
     it.u = __fadd_rn(__fdiv_rn(atan2f(n.z, n.x), __fmul_rn(2.f, CUDART_PI_F)), 0.5f);

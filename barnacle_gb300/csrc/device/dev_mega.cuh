@@ -21,7 +21,7 @@ __device__ __forceinline__ int find_view(const long long* __restrict__ offsets, 
   return v;
 }
 
-template <bool kWT, int kWalk, int kInteg>
+template <bool kWT, int kWalk, int kInteg, bool kSimple = false>
 __global__ void __launch_bounds__(128) k_pt_mega(DevScene s, MegaParams p) {
   constexpr bool kCount = kWalk == kWalkCount;
   // scenes walked binary are small and shading-bound: one out-of-line walk keeps the kernel in
@@ -47,11 +47,11 @@ __global__ void __launch_bounds__(128) k_pt_mega(DevScene s, MegaParams p) {
                                       static_cast<uint32_t>(p.frame_id * p.spp + sid))};
       const float upx = smp.next(), upy = smp.next();
       const float ulx = smp.next(), uly = smp.next();
-      const Ray ray = camera_ray(v, x, y, upx, upy, ulx, uly);
+      const Ray ray = camera_ray<kSimple>(v, x, y, upx, upy, ulx, uly);
       V3 L;
       if (kInteg == BN_INTEGRATOR_NORMAL) L = li_normal<kWT, kWalk, kOutline>(s, ray, &pc);
       else if (kInteg == BN_INTEGRATOR_DIRECT) L = li_direct<kWT, kWalk, IndepSampler, kOutline>(s, ray, smp, &pc);
-      else L = li_path<kWT, false, kWalk, IndepSampler, kOutline>(s, ray, smp, p.max_depth, p.rr_depth, &pc);
+      else L = li_path<kWT, false, kWalk, IndepSampler, kOutline, kSimple>(s, ray, smp, p.max_depth, p.rr_depth, &pc);
       acc = fma3(mk(inv_spp, inv_spp, inv_spp), L, acc);
       ++paths;
     }

@@ -54,6 +54,10 @@ __device__ __forceinline__ void concentric_disk(float ux, float uy, float* dx, f
   *dy = __fmul_rn(r, sinf(theta));
 }
 
+// kSimple (here and below): a scene of Lambertian triangle meshes, the uniform light sampler and
+// pinhole views only; the specialised code leaves the other branches out, which keeps a path
+// loop small enough for the instruction cache.
+template <bool kSimple = false>
 __device__ __forceinline__ Ray camera_ray(const DevView& v, int x, int y, float upx, float upy, float ulx, float uly) {
   // PinholeCamera.GenerateRay (Pinhole.fs:12-27): ((ul + (x + u.x) du) + (y + u.y) dv), normalised
   const float a = __fadd_rn(static_cast<float>(x), upx), b = __fadd_rn(static_cast<float>(y), upy);
@@ -63,7 +67,7 @@ __device__ __forceinline__ Ray camera_ray(const DevView& v, int x, int y, float 
   Ray r;
   r.o = mk(0.f, 0.f, 0.f);
   r.d = normalize(pl);
-  if (v.cam_type == BN_CAM_THIN_LENS && v.aperture > 0.f) {
+  if (!kSimple && v.cam_type == BN_CAM_THIN_LENS && v.aperture > 0.f) {
     // ThinLensCamera.GenerateRay (ThinLens.fs:26-35)
     float dx, dy;
     concentric_disk(ulx, uly, &dx, &dy);
@@ -134,9 +138,10 @@ __device__ __forceinline__ BsdfEval pbr_eval(V3 base, float alpha, float metalli
   return e;
 }
 
+template <bool kSimple = false>
 __device__ __forceinline__ BsdfEval bsdf_eval(const DevMaterial& m, V3 wo, V3 wi) {
   BsdfEval e{{0.f, 0.f, 0.f}, 0.f};
-  if (m.type == kMatLambertian) {
+  if (kSimple || m.type == kMatLambertian) {
     // Lambertian.Eval (Lambertian.fs:11-16)
     if (__fmul_rn(wi.z, wo.z) < 0.f || fminf(fabsf(wi.z), fabsf(wo.z)) < 1e-6f) return e;
     const float pdf = __fdiv_rn(fabsf(wi.z), kPi);
@@ -156,10 +161,11 @@ __device__ __forceinline__ V3 cosine_dir(float u0, float u1) {
   return {__fmul_rn(sin_t, cp), __fmul_rn(sin_t, sp), cos_t};
 }
 
+template <bool kSimple = false>
 __device__ __forceinline__ BsdfSample bsdf_sample(const DevMaterial& m, V3 wo, float u_lobe, float u0, float u1) {
   BsdfSample s;
   const V3 base = mk(m.base[0], m.base[1], m.base[2]);
-  if (m.type == kMatLambertian) {
+  if (kSimple || m.type == kMatLambertian) {
     // Lambertian.Sample (Lambertian.fs:18-26): cosine lobe mirrored to wo's side
     V3 wi = cosine_dir(u0, u1);
     const float pdf = __fdiv_rn(wi.z, kPi);
@@ -278,11 +284,12 @@ struct LightSample {
 
 // LightSamplerBase.Sample: UniformLightSampler.Sample (Uniform.fs:13-29) or the alias-table
 // sampler over emissive triangles
+template <bool kSimple = false>
 __device__ __forceinline__ LightSample sample_light(const DevScene& s, V3 p, float u_select, float ux, float uy) {
   SurfacePoint sp;
   int light;
   float sel;  // light-choice factor dividing the pdf (N for uniform, 1 for alias)
-  if (s.light_sampler == BN_LIGHTS_ALIAS_TRIANGLES) {
+  if (!kSimple && s.light_sampler == BN_LIGHTS_ALIAS_TRIANGLES) {
     const int n = s.n_tri_lights;
     const float u = __fmul_rn(u_select, static_cast<float>(n));
     int idx = min(static_cast<int>(u), n - 1);
@@ -303,7 +310,7 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& s, V3 p, flo
     const int id = min(static_cast<int>(us), n - 1);
     us = __fsub_rn(us, static_cast<float>(id));
     const DevInstance* I = s.inst + __ldg(&s.light_inst[id]);
-    if (__ldg(&I->prim_type) == kPrimSphere) {
+    if (!kSimple && __ldg(&I->prim_type) == kPrimSphere) {
       sp = sphere_sample(I, ux, uy);
     } else {
       // MeshInstance.Sample (Mesh.fs:289-298): the reference alias table picks int(u * n)
@@ -333,13 +340,14 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& s, V3 p, flo
 
 // LightSamplerBase.Eval (Uniform.fs:40-49): radiance and solid-angle pdf of an emitter hit
 // seen from `origin`
+template <bool kSimple = false>
 __device__ __forceinline__ void eval_light(const DevScene& s, V3 origin, const Interaction& it, V3* L, float* pdf) {
   const DevInstance* I = s.inst + it.inst;
   const V3 dp = sub(origin, it.p);
   const V3 wo = normalize(dp);
   const float cos_wo = dot(it.f.n, wo);
   float pdf_surface, sel;
-  if (s.light_sampler == BN_LIGHTS_ALIAS_TRIANGLES) {
+  if (!kSimple && s.light_sampler == BN_LIGHTS_ALIAS_TRIANGLES) {
     const int e = __ldg(&I->light_entry_base) + it.tri;
     V3 p0, p1, p2;
     world_tri(s, I, it.tri, &p0, &p1, &p2);
@@ -347,7 +355,7 @@ __device__ __forceinline__ void eval_light(const DevScene& s, V3 origin, const I
     pdf_surface = __fmul_rn(__ldg(&s.tri_lights[e].pmf), area_pdf);
     sel = 1.f;
   } else {
-    if (__ldg(&I->prim_type) == kPrimSphere) {
+    if (!kSimple && __ldg(&I->prim_type) == kPrimSphere) {
       // SphereInstance.EvalPDF (Sphere.fs:115-126)
       float4 w2o[3];
       load_xf(I->w2o, w2o);
@@ -393,7 +401,7 @@ struct PathCounters {
 // Draw order per bounce: u_select, u_light.xy (NEE), u_lobe, u_bsdf.xy, then u_rr if depth >=
 // rr_depth (PathTracing) / always (PSSMLT).  Reciprocal estimates are exact reciprocals here.
 // kOutline: one out-of-line walk for both queries (see trace_walk_outline).
-template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false>
+template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false>
 __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int max_depth, int rr_depth, PathCounters* pc) {
   constexpr bool kCount = kWalk == kWalkCount;
   V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
@@ -403,12 +411,12 @@ __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int 
     HitRec h;
     if (kCount) pc->rays++;
     if (!trace_closest<kWT, kWalk, kOutline>(s, ray, CUDART_INF_F, &h, &pc->tc)) break;
-    const Interaction it = make_interaction(s, ray, h);
+    const Interaction it = make_interaction<kSimple>(s, ray, h);
     const DevInstance* I = s.inst + it.inst;
     if (__ldg(&I->light) >= 0) {
       V3 le;
       float pdf_l;
-      eval_light(s, ray.o, it, &le, &pdf_l);
+      eval_light<kSimple>(s, ray.o, it, &le, &pdf_l);
       const float mis = depth == 0 ? 1.f : __fmul_rn(pdf_bsdf, __frcp_rn(__fadd_rn(pdf_l, pdf_bsdf)));
       L = fma3(beta, scale(mis, le), L);
     }
@@ -422,7 +430,7 @@ __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int 
     if (!kFixed7) { u_sel = smp.next(); ulx = smp.next(); uly = smp.next(); }
     const DevMaterial m = s.mats[mat];
     const V3 wo_w = neg(ray.d);
-    const LightSample ls = sample_light(s, it.p, u_sel, ulx, uly);
+    const LightSample ls = sample_light<kSimple>(s, it.p, u_sel, ulx, uly);
     const float dist = length(sub(ls.p, it.p));
     if (ls.pdf != 0.f) {
       Ray sh;
@@ -430,12 +438,12 @@ __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int 
       sh.d = ls.wi;
       if (kCount) pc->rays++;
       if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
-        const BsdfEval be = bsdf_eval(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
+        const BsdfEval be = bsdf_eval<kSimple>(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
         L = fma3(mul(beta, be.f), scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L), L);
       }
     }
     if (!kFixed7) { u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); }
-    const BsdfSample bs = bsdf_sample(m, to_local(it.f, wo_w), u_lobe, ubx, uby);
+    const BsdfSample bs = bsdf_sample<kSimple>(m, to_local(it.f, wo_w), u_lobe, ubx, uby);
     if (bs.pdf == 0.f) break;
     pdf_bsdf = bs.pdf;
     ray.o = it.p;

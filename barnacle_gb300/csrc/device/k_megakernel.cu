@@ -35,6 +35,12 @@ cudaError_t launch_megakernel(const DevScene& s, const MegaParams& p, cudaStream
   const long long grid = (p.n_items + bs - 1) / bs;
   if (p.integrator == BN_INTEGRATOR_NORMAL || p.integrator == BN_INTEGRATOR_DIRECT)
     return launch_megakernel_simple(s, p, st);
+  if (p.simple && !p.count && !s.wide) {
+    // Lambertian meshes, uniform lights, pinhole views: the specialised path loop
+    if (p.watertight) k_pt_mega<true, kWalkBinary, BN_INTEGRATOR_PATH, true><<<grid, bs, 0, st>>>(s, p);
+    else k_pt_mega<false, kWalkBinary, BN_INTEGRATOR_PATH, true><<<grid, bs, 0, st>>>(s, p);
+    return cudaGetLastError();
+  }
   dispatch_walk<true>(s, p.watertight, p.count, [&](auto wt, auto walk) {
     k_pt_mega<decltype(wt)::value, decltype(walk)::value, BN_INTEGRATOR_PATH><<<grid, bs, 0, st>>>(s, p);
   });

@@ -55,6 +55,7 @@ struct MegaParams {
   int spp, chunks, spc;      // samples per pixel, chunks per pixel, samples per chunk
   int max_depth, rr_depth, frame_id;
   int integrator;            // bn_integrator_type: PATH, NORMAL or DIRECT
+  bool simple;               // Lambertian meshes, uniform light sampler, pinhole views only
   bool watertight;
   bool count;
   float4* partial;           // n_items partial sums (scratch)

@@ -383,3 +383,27 @@ def test_no_scene_and_bad_scene_errors():
             s.instances[i].light = -1
         with pytest.raises(BarnacleError, match="No light primitives"):
             c.upload(b)
+
+
+def test_simple_scene_specialisation_renders_the_same(ctx):
+    """A scene of Lambertian meshes with the uniform light sampler and pinhole views runs a path
+    loop compiled without the other materials, spheres and thin lenses; it must render the same
+    floats as the general loop, which an unused mirror material switches back on."""
+    from barnacle_gb300.capi import bn_material_desc
+    b = Bundle.generate("cornell", 1)
+    r = b.render
+    r.spp = 8
+    ctx.upload(b)
+    simple = ctx.render(r, b.views[0])[0]
+    s = b.scene.contents
+    mats = (bn_material_desc * (s.n_materials + 1))(*[s.materials[i] for i in range(s.n_materials)])
+    mats[s.n_materials].type = capi.BN_MAT_MIRROR
+    keep = s.materials, s.n_materials
+    s.materials, s.n_materials = C.cast(mats, type(s.materials)), s.n_materials + 1
+    try:
+        ctx.upload(b)
+        general = ctx.render(r, b.views[0])[0]
+    finally:
+        s.materials, s.n_materials = keep
+    assert simple.max() > 0.5
+    assert np.array_equal(simple.view(np.uint32), general.view(np.uint32))
