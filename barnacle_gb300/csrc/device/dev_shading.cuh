@@ -396,68 +396,93 @@ struct PathCounters {
   TraceCounters tc;
 };
 
-// PathTracingIntegrator.Li (Extensions/Integrator/PathTracing.fs:14-81) and, with kFixed7,
-// PSSMLTIntegrator.Li (PSSMLT.fs:172-245), which draws 7 samples per bounce in a fixed order.
+// The state of one path between bounces (PathTracingIntegrator.Li's loop variables).
+struct PathState {
+  Ray ray;
+  V3 L, beta;
+  float pdf_bsdf;
+  int depth;
+};
+
+__device__ __forceinline__ void path_begin(PathState& ps, const Ray& ray) {
+  ps.ray = ray;
+  ps.L = mk(0.f, 0.f, 0.f);
+  ps.beta = mk(1.f, 1.f, 1.f);
+  ps.pdf_bsdf = 0.f;
+  ps.depth = 0;
+}
+
+// One iteration of PathTracingIntegrator.Li's bounce loop (Extensions/Integrator/PathTracing.fs:
+// 14-81) and, with kFixed7, of PSSMLTIntegrator.Li (PSSMLT.fs:172-245), which draws 7 samples per
+// bounce in a fixed order; returns true once the path has ended (ps.L holds its radiance).
 // Draw order per bounce: u_select, u_light.xy (NEE), u_lobe, u_bsdf.xy, then u_rr if depth >=
 // rr_depth (PathTracing) / always (PSSMLT).  Reciprocal estimates are exact reciprocals here.
 // kOutline: one out-of-line walk for both queries (see trace_walk_outline).
 template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false>
-__device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int max_depth, int rr_depth, PathCounters* pc) {
+__device__ __forceinline__ bool li_bounce(const DevScene& s, PathState& ps, Smp& smp, int max_depth, int rr_depth,
+                                          PathCounters* pc) {
   constexpr bool kCount = kWalk == kWalkCount;
-  V3 L = mk(0.f, 0.f, 0.f), beta = mk(1.f, 1.f, 1.f);
-  float pdf_bsdf = 0.f;
-  int depth = 0;
-  while (depth < max_depth) {
-    HitRec h;
-    if (kCount) pc->rays++;
-    if (!trace_closest<kWT, kWalk, kOutline>(s, ray, CUDART_INF_F, &h, &pc->tc)) break;
-    const Interaction it = make_interaction<kSimple>(s, ray, h);
-    const DevInstance* I = s.inst + it.inst;
-    if (__ldg(&I->light) >= 0) {
-      V3 le;
-      float pdf_l;
-      eval_light<kSimple>(s, ray.o, it, &le, &pdf_l);
-      const float mis = depth == 0 ? 1.f : __fmul_rn(pdf_bsdf, __frcp_rn(__fadd_rn(pdf_l, pdf_bsdf)));
-      L = fma3(beta, scale(mis, le), L);
-    }
-    float u_sel, ulx, uly, u_lobe, ubx, uby, u_rr = 0.f;
-    const int mat = hit_material(s, it);
-    if (kFixed7) {
-      u_sel = smp.next(); ulx = smp.next(); uly = smp.next();
-      u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); u_rr = smp.next();
-    }
-    if (mat < 0) break;
-    if (!kFixed7) { u_sel = smp.next(); ulx = smp.next(); uly = smp.next(); }
-    const DevMaterial m = s.mats[mat];
-    const V3 wo_w = neg(ray.d);
-    const LightSample ls = sample_light<kSimple>(s, it.p, u_sel, ulx, uly);
-    const float dist = length(sub(ls.p, it.p));
-    if (ls.pdf != 0.f) {
-      Ray sh;
-      sh.o = it.p;
-      sh.d = ls.wi;
-      if (kCount) pc->rays++;
-      if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
-        const BsdfEval be = bsdf_eval<kSimple>(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
-        L = fma3(mul(beta, be.f), scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L), L);
-      }
-    }
-    if (!kFixed7) { u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); }
-    const BsdfSample bs = bsdf_sample<kSimple>(m, to_local(it.f, wo_w), u_lobe, ubx, uby);
-    if (bs.pdf == 0.f) break;
-    pdf_bsdf = bs.pdf;
-    ray.o = it.p;
-    ray.d = to_world(it.f, bs.wi);
-    beta = scale(__frcp_rn(bs.pdf), mul(beta, bs.f));
-    if (depth >= rr_depth) {
-      const float q = fminf(1.f, fmaxf(beta.x, fmaxf(beta.y, beta.z)));
-      if (!kFixed7) u_rr = smp.next();
-      if (u_rr < q) beta = scale(__frcp_rn(q), beta);
-      else break;
-    }
-    depth++;
+  if (ps.depth >= max_depth) return true;
+  Ray& ray = ps.ray;
+  HitRec h;
+  if (kCount) pc->rays++;
+  if (!trace_closest<kWT, kWalk, kOutline>(s, ray, CUDART_INF_F, &h, &pc->tc)) return true;
+  const Interaction it = make_interaction<kSimple>(s, ray, h);
+  const DevInstance* I = s.inst + it.inst;
+  if (__ldg(&I->light) >= 0) {
+    V3 le;
+    float pdf_l;
+    eval_light<kSimple>(s, ray.o, it, &le, &pdf_l);
+    const float mis = ps.depth == 0 ? 1.f : __fmul_rn(ps.pdf_bsdf, __frcp_rn(__fadd_rn(pdf_l, ps.pdf_bsdf)));
+    ps.L = fma3(ps.beta, scale(mis, le), ps.L);
   }
-  return L;
+  float u_sel, ulx, uly, u_lobe, ubx, uby, u_rr = 0.f;
+  const int mat = hit_material(s, it);
+  if (kFixed7) {
+    u_sel = smp.next(); ulx = smp.next(); uly = smp.next();
+    u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); u_rr = smp.next();
+  }
+  if (mat < 0) return true;
+  if (!kFixed7) { u_sel = smp.next(); ulx = smp.next(); uly = smp.next(); }
+  const DevMaterial m = s.mats[mat];
+  const V3 wo_w = neg(ray.d);
+  const LightSample ls = sample_light<kSimple>(s, it.p, u_sel, ulx, uly);
+  const float dist = length(sub(ls.p, it.p));
+  if (ls.pdf != 0.f) {
+    Ray sh;
+    sh.o = it.p;
+    sh.d = ls.wi;
+    if (kCount) pc->rays++;
+    if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
+      const BsdfEval be = bsdf_eval<kSimple>(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
+      ps.L = fma3(mul(ps.beta, be.f), scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L), ps.L);
+    }
+  }
+  if (!kFixed7) { u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); }
+  const BsdfSample bs = bsdf_sample<kSimple>(m, to_local(it.f, wo_w), u_lobe, ubx, uby);
+  if (bs.pdf == 0.f) return true;
+  ps.pdf_bsdf = bs.pdf;
+  ray.o = it.p;
+  ray.d = to_world(it.f, bs.wi);
+  ps.beta = scale(__frcp_rn(bs.pdf), mul(ps.beta, bs.f));
+  if (ps.depth >= rr_depth) {
+    const float q = fminf(1.f, fmaxf(ps.beta.x, fmaxf(ps.beta.y, ps.beta.z)));
+    if (!kFixed7) u_rr = smp.next();
+    if (u_rr < q) ps.beta = scale(__frcp_rn(q), ps.beta);
+    else return true;
+  }
+  ps.depth++;
+  return false;
+}
+
+// the whole path: PathTracingIntegrator.Li / PSSMLTIntegrator.Li
+template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false>
+__device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int max_depth, int rr_depth, PathCounters* pc) {
+  PathState ps;
+  path_begin(ps, ray);
+  while (!li_bounce<kWT, kFixed7, kWalk, Smp, kOutline, kSimple>(s, ps, smp, max_depth, rr_depth, pc)) {
+  }
+  return ps.L;
 }
 
 // NormalIntegrator.Li (Extensions/Integrator/Normal.fs:10-17): 0.5 (n + 1) of the shading normal
