@@ -102,3 +102,45 @@ def test_json_scene_pssmlt_matches_oracle(ctx):
     assert abs(st.bootstrap_b / cb - 1) < 0.05
     assert abs(st.accepted / acc - 1) < 0.05 and st.proposed == prop
     assert abs(gi.sum() / ci.sum() - 1) < 0.05
+
+
+@pytest.mark.parametrize("mode", [capi.BN_MODE_MEGAKERNEL, capi.BN_MODE_WAVEFRONT])
+def test_json_scene_normal_integrator_matches_oracle(ctx, mode):
+    """The Normal integrator on analytic spheres seen through the thin lens: the lens sample goes
+    through sin/cos, so a pixel's normal agrees to float rounding rather than bit for bit."""
+    b = Bundle.load_json(str(SCENES / "spheres_thinlens.json"))
+    ctx.upload(b)
+    r = b.render
+    r.integrator = capi.BN_INTEGRATOR_NORMAL
+    r.mode = mode
+    r.spp = 2
+    v = b.views[0]
+    img = ctx.render(r, v)[0]
+    ref, _ = pyoracle.Scene(b.scene).render_pt(r, v)
+    assert (ref > 0).mean() > 0.15 and ref.max() <= 1.0  # the spheres cover a fifth of the film
+    close = np.abs(img - ref) <= 1e-4
+    assert close.all(axis=2).mean() > 0.995
+
+
+def test_json_scene_direct_integrator_statistically_matches_oracle(ctx):
+    """The Direct integrator with an emissive sphere (SphereInstance.Sample / EvalPDF)."""
+    b = Bundle.load_json(str(SCENES / "sphere_light.json"))
+    ctx.upload(b)
+    r = b.render
+    r.integrator = capi.BN_INTEGRATOR_DIRECT
+    r.mode = capi.BN_MODE_MEGAKERNEL
+    r.spp = 8
+    v = b.views[0]
+    o = pyoracle.Scene(b.scene)
+    gpu, cpu = [], []
+    for f in range(8):
+        r.frame_id = f
+        gpu.append(ctx.render(r, v)[0])
+        r.frame_id = 500 + f
+        cpu.append(o.render_pt(r, v)[0])
+    g = np.stack(gpu).astype(np.float64)
+    c = np.stack(cpu).astype(np.float64)
+    se = np.sqrt(g.var(0, ddof=1) / len(g) + c.var(0, ddof=1) / len(c))
+    z = np.abs(g.mean(0) - c.mean(0)) / np.maximum(se, 1e-12)
+    assert c.mean() > 0.01
+    assert (z[se > 0] > 3).mean() < 0.02
