@@ -236,8 +236,10 @@ def run_reference(args, world, rank, dist):
     views = b.views
     threads = os.cpu_count() or 1
     r = b.render
-    sample_views = views[:4]
-    crop = 48 if args.workload == "instances" else 32
+    # the same sample as the GPU arm's cpu_baseline (centre crops of the first views), at the
+    # step's samples per pixel
+    nv, crop, _ = WORKLOADS[args.workload][2]
+    sample_views = views[:nv]
     for _ in range(args.warmup):
         cpu_sample_render(b, b.render, args.spp_per_step, sample_views[:1], 16, threads)
     paths, secs = 0, 0.0
