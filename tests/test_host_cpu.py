@@ -252,9 +252,13 @@ def test_json_loader_errors(tmp_path):
         Bundle.generate("no-such-workload")
 
 
-@pytest.mark.skipif(not Path("/root/reference/Asset/cbox.json").exists(), reason="reference asset not mounted")
+# the reference checkout next to this repository, when it is mounted (never on a GPU machine)
+CBOX = ROOT.parent / "reference" / "Asset" / "cbox.json"
+
+
+@pytest.mark.skipif(not CBOX.exists(), reason="reference asset not mounted")
 def test_json_loader_reads_reference_cbox():
-    b = Bundle.load_json("/root/reference/Asset/cbox.json")
+    b = Bundle.load_json(str(CBOX))
     s = b.scene.contents
     assert s.n_instances == 9 and s.n_primitives == 9
     assert b.render.integrator == capi.BN_INTEGRATOR_PSSMLT and b.render.spp == 16
