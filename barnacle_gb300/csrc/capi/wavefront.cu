@@ -246,7 +246,7 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
     const bool wt = d->flags & BN_RENDER_WATERTIGHT;
     if (w->tuned_generation != ctx->scene_generation || w->tuned_watertight != wt) {
       // autotune on a truncated render of the same views: pool size x blocks-per-SM cap
-      const int pools[4] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+      const int pools[5] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24};
       const int caps[2] = {0, 2};
       const long long sample = std::min<long long>(total, 24LL << 20);
       float best = 1e30f;
