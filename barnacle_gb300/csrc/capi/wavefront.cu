@@ -248,7 +248,7 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
       // autotune on a truncated render of the same views: pool size x blocks-per-SM cap
       const int pools[5] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24};
       const int caps[2] = {0, 2};
-      const long long sample = std::min<long long>(total, 24LL << 20);
+      const long long sample = std::min<long long>(total, 32LL << 20);  // two fills of the largest pool
       float best = 1e30f;
       for (int pi : pools)
         for (int ci : caps) {
