@@ -115,11 +115,22 @@ struct Collapse {
     for (int k = 0; k < 6; ++k) r[k] = make_float4(box[k][0], box[k][1], box[k][2], box[k][3]);
     float4 rf, mt;
     std::memcpy(&rf, ref, 16);
+    // slot order per ray octant (bit a of the octant: d[a] > 0): the near child's pair first (left
+    // when d[axis of g] > 0), each pair ordered by its child's split axis; 2 bits per slot
+    unsigned orders[2] = {0u, 0u};
+    for (int oct = 0; oct < 8; ++oct) {
+      const bool lf = (oct >> (axis[0] & 3)) & 1;
+      const bool fa = (oct >> (axis[lf ? 1 : 2] & 3)) & 1;
+      const bool fb = (oct >> (axis[lf ? 2 : 1] & 3)) & 1;
+      const int pa = lf ? 0 : 2, pb = 2 - pa;
+      const unsigned v0 = pa + (fa ? 0 : 1), v1 = pa + (fa ? 1 : 0), v2 = pb + (fb ? 0 : 1), v3 = pb + (fb ? 1 : 0);
+      orders[oct >> 2] |= (v0 | (v1 << 2) | (v2 << 4) | (v3 << 6)) << (8 * (oct & 3));
+    }
     const int meta[4] = {static_cast<int>(counts),
                          static_cast<int>(leaf_mask | (static_cast<unsigned>(axis[0] & 3) << 4) |
                                           (static_cast<unsigned>(axis[1] & 3) << 6) |
                                           (static_cast<unsigned>(axis[2] & 3) << 8)),
-                         0, 0};
+                         static_cast<int>(orders[0]), static_cast<int>(orders[1])};
     std::memcpy(&mt, meta, 16);
     r[6] = rf;
     r[7] = mt;

@@ -122,9 +122,10 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   // both queues sorted by ray key: on the 1,024-instance workload 111.5 M paths/s against 110.0
   // (ray queue only) and 107.9 (neither)
   const bool sort = true, sort_shadow = true;
+  const bool count = d->flags & BN_RENDER_COUNT;
   if (w->shape_cap != cap || w->shape.watertight != wt || w->shape.wide != wide || w->shape.sort != sort ||
-      w->shape.sort_shadow != sort_shadow) {
-    w->shape = bn::wf_launch_shape(wt, wide, sort, sort_shadow, cap);
+      w->shape.sort_shadow != sort_shadow || w->shape.count != count) {
+    w->shape = bn::wf_launch_shape(wt, wide, sort, sort_shadow, count, cap);
     w->shape_cap = cap;
     if (w->exec) {
       cudaGraphExecDestroy(w->exec);
@@ -178,6 +179,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.q_bins = w->q_bins.as<int>();
   p.shadow = w->shadow.as<float4>();
   p.counters = w->counters.as<int>();
+  p.trace_counters = ctx->counters.ptr;
   p.work_next = w->work_next.as<unsigned long long>();
   p.film_acc = w->film_acc.as<double>();
   p.film_out = ctx->film.as<float>();
@@ -242,7 +244,7 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
   }
   const bool use_graph = !(d->flags & BN_RENDER_NO_GRAPH);
   int pool = d->queue_capacity, cap = d->block_size;  // block_size doubles as the blocks/SM cap
-  if (pool <= 0 && cap <= 0) {
+  if (pool <= 0 && cap <= 0 && !(d->flags & BN_RENDER_COUNT)) {  // a counting render is a one-off: no tuning
     const bool wt = d->flags & BN_RENDER_WATERTIGHT;
     if (w->tuned_generation != ctx->scene_generation || w->tuned_watertight != wt) {
       // autotune on a truncated render of the same views: pool size x blocks-per-SM cap

@@ -45,11 +45,17 @@ __device__ __forceinline__ bool box_hit_t(V3 bmin, V3 bmax, const Ray& r, V3 inv
 
 enum : int { kTravNode = 0, kTravTri = 1, kTravInst = 2, kTravDone = 3 };
 
+// the reference's near-child test d[axis] > 0 for the three axes at once (a zero or NaN component
+// is not > 0, as in BVH.fs)
+__device__ __forceinline__ int octant(V3 d) { return int(d.x > 0.f) | (int(d.y > 0.f) << 1) | (int(d.z > 0.f) << 2); }
+
 struct Trav {
   Ray wr;            // world ray
   V3 winv;
+  int woct;          // octant of the world direction: bit a set when d[a] > 0
   Ray orr;           // object-space ray of the instance being walked
   V3 oinv;
+  int ooct;          // the same for the object-space direction
   WtRay wt;
   float t;
   NodeRec n;         // current interior node (kTravNode), its box already passed
@@ -143,6 +149,7 @@ template <int kWalk>
 __device__ __forceinline__ void trav_init(Trav& tr, const DevScene& s, const Ray& ray, float tmax, TraceCounters* cnt) {
   tr.wr = ray;
   tr.winv = inv_dir(ray.d);
+  tr.woct = octant(ray.d);
   tr.t = tmax;
   tr.found = false;
   tr.hit.inst = -1;
@@ -190,18 +197,17 @@ __device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, 
   const bool h3 = box_hit_t(mk(lx.w, ly.w, lz.w), mk(hx.w, hy.w, hz.w), r, inv, tr.t, &e3);
   const int hm = int(h0) | (int(h1) << 1) | (int(h2) << 2) | (int(h3) << 3);
   if (!hm) return kStepPop;
-  // the binary walk's order: the near child's slots, then the far child's, each pair ordered by
-  // that child's own split axis (BVH.fs near-child rule at both levels)
+  // the binary walk's order (the near child's slots, then the far child's, each pair ordered by
+  // that child's own split axis: BVH.fs near-child rule at both levels) depends on the ray only
+  // through its octant; the upload stored the slot order of each octant, 8 bits per octant
   const int m = meta.y;
-  const bool lf = comp(r.d, (m >> 4) & 3) > 0.f;
-  const bool fa = comp(r.d, lf ? ((m >> 6) & 3) : ((m >> 8) & 3)) > 0.f;
-  const bool fb = comp(r.d, lf ? ((m >> 8) & 3) : ((m >> 6) & 3)) > 0.f;
-  const int pa = lf ? 0 : 2, pb = 2 - pa;
+  const int oct = tr.level ? tr.ooct : tr.woct;
+  const unsigned order = (static_cast<unsigned>(oct & 4 ? meta.w : meta.z) >> (8 * (oct & 3))) & 0xffu;
   int v[4];
-  v[0] = pa + (fa ? 0 : 1);
-  v[1] = pa + (fa ? 1 : 0);
-  v[2] = pb + (fb ? 0 : 1);
-  v[3] = pb + (fb ? 1 : 0);
+  v[0] = order & 3;
+  v[1] = (order >> 2) & 3;
+  v[2] = (order >> 4) & 3;
+  v[3] = (order >> 6) & 3;
   int first = 3;
 #pragma unroll
   for (int k = 2; k >= 0; --k)
@@ -329,6 +335,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
           }
         } else {
           tr.oinv = inv_dir(tr.orr.d);
+          tr.ooct = octant(tr.orr.d);
           if (kWT) tr.wt = wt_setup(tr.orr.d);
           const int base = ids.y;
           float te;

@@ -11,7 +11,9 @@
 //             the right child's.  (lo.x[4], lo.y[4], lo.z[4], hi.x[4], hi.y[4], hi.z[4]) slot
 //             boxes, int4 ref (node4 index of an interior slot, first item of a leaf slot),
 //             int4 meta (x: leaf item count, 8 bits per slot; y: leaf mask bits 0-3, split axis
-//             of the node << 4, of its left child << 6, of its right child << 8).  Unused slots
+//             of the node << 4, of its left child << 6, of its right child << 8; z, w: the slot
+//             visit order for each of the 8 ray octants, 8 bits = 4 x 2-bit slots per octant,
+//             octants 0-3 in z, 4-7 in w).  Unused slots
 //             have NaN boxes, which no ray enters.  TLAS records first (root at 0 when the TLAS
 //             root is interior), then every BLAS at DevInstance::node4_root.  Built when the
 //             scene is walked wide (DevScene::wide).

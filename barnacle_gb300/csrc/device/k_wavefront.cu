@@ -19,6 +19,7 @@
 // differs.  Kernels are persistent grid-stride loops whose trip counts come from device counters,
 // so one captured graph serves every iteration.
 #include "dev_shading.cuh"
+#include "launch.hpp"
 #include "wavefront.hpp"
 
 namespace bn {
@@ -136,6 +137,24 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
   }
 }
 
+// a counting walk's totals: one atomic per warp and counter (every lane of the warp reaches it)
+__device__ __forceinline__ void add_trace_counts(void* out, unsigned long long rays, const TraceCounters& tc) {
+  unsigned long long r = rays, nn = tc.nodes, tt = tc.tris, ii = tc.insts;
+  for (int o = 16; o > 0; o >>= 1) {
+    r += __shfl_down_sync(0xffffffffu, r, o);
+    nn += __shfl_down_sync(0xffffffffu, nn, o);
+    tt += __shfl_down_sync(0xffffffffu, tt, o);
+    ii += __shfl_down_sync(0xffffffffu, ii, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    DevCounters* c = static_cast<DevCounters*>(out);
+    atomicAdd(&c->rays, r);
+    atomicAdd(&c->nodes, nn);
+    atomicAdd(&c->tris, tt);
+    atomicAdd(&c->insts, ii);
+  }
+}
+
 // Persistent lanes with dynamic ray fetch: a lane whose ray finished claims the next queued ray
 // (one atomic per warp for all lanes that need one) and keeps stepping, so a warp never waits
 // out its slowest ray with idle lanes while work remains in the queue.  Finished lanes wait until
@@ -163,7 +182,8 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
   int sn[kStackSize];
   float st[kStackSize];
   Trav tr;
-  TraceCounters tc;
+  TraceCounters tc{0, 0, 0};
+  unsigned long long nrays = 0;  // rays this lane walked (counting walks)
   int slot = -1;
   bool have = false, pending = false;
   for (;;) {
@@ -205,6 +225,7 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
         ray.d = mk(d.x, d.y, d.z);
         trav_init<kWalk>(tr, s, ray, CUDART_INF_F, &tc);
         have = true;
+        ++nrays;
       }
     }
     // a walk can end at init (root box missed)
@@ -213,6 +234,19 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
       pending = true;
     }
   }
+  if (kWalk == kWalkCount) add_trace_counts(p.trace_counters, nrays, tc);
+}
+
+// The shadow kernel adds fma(a, b, L) per channel when the shadow ray is unoccluded.  Where every
+// a*b is exactly zero (a factor 0 and the other finite) and L holds no -0, that leaves L as it is,
+// so the ray need not be queued: below-horizon light samples (f = 0) and the back of one-sided
+// lights (L_e = 0) cost no traversal, and the path's radiance keeps the same bits.
+__device__ __forceinline__ bool shadow_contributes(V3 a, V3 b, V3 L) {
+  auto zero = [](float x, float y, float l) {
+    const bool prod0 = (x == 0.f && isfinite(y)) || (y == 0.f && isfinite(x));
+    return prod0 && !(l == 0.f && signbit(l));
+  };
+  return !(zero(a.x, b.x, L.x) && zero(a.y, b.y, L.y) && zero(a.z, b.z, L.z));
 }
 
 // DirectIntegrator.Li (Extensions/Integrator/Direct.fs:10-40) as two wavefront vertices.  At the
@@ -252,7 +286,7 @@ __device__ __forceinline__ void shade_direct(const WfParams& p, const DevScene& 
   *sh_d = make_float4(ls.wi.x, ls.wi.y, ls.wi.z, __int_as_float(slot));
   *sh_a = make_float4(be.f.x, be.f.y, be.f.z, 0.f);
   *sh_b = make_float4(bb.x, bb.y, bb.z, 0.f);
-  *shadow = true;
+  *shadow = shadow_contributes(be.f, bb, *L);
   const float u_lobe = smp.next(), ubx = smp.next(), uby = smp.next();
   const BsdfSample bs = bsdf_sample(mt, to_local(it.f, wo_w), u_lobe, ubx, uby);
   const V3 nd = to_world(it.f, bs.wi);
@@ -337,7 +371,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
             sh_d = make_float4(ls.wi.x, ls.wi.y, ls.wi.z, __int_as_float(slot));
             sh_a = make_float4(a.x, a.y, a.z, 0.f);
             sh_b = make_float4(bb.x, bb.y, bb.z, 0.f);
-            shadow = true;
+            shadow = shadow_contributes(a, bb, L);
           }
           const float u_lobe = smp.next(), ubx = smp.next(), uby = smp.next();
           const BsdfSample bs = bsdf_sample(mt, to_local(it.f, wo_w), u_lobe, ubx, uby);
@@ -397,7 +431,8 @@ __global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict
   int sn[kStackSize];
   float st[kStackSize];
   Trav tr;
-  TraceCounters tc;
+  TraceCounters tc{0, 0, 0};
+  unsigned long long nrays = 0;  // rays this lane walked (counting walks)
   int rec = -1;
   bool have = false, pending = false;
   for (;;) {
@@ -426,6 +461,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict
         ray.d = mk(d.x, d.y, d.z);
         trav_init<kWalk>(tr, p.scene, ray, o.w, &tc);
         have = true;
+        ++nrays;
       }
     }
     if (have && (tr.mode == kTravDone || trav_step<kAnyHit, kWT, kWalk>(tr, p.scene, sn, st, &tc))) {
@@ -433,6 +469,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict
       pending = true;
     }
   }
+  if (kWalk == kWalkCount) add_trace_counts(p.trace_counters, nrays, tc);
 }
 
 // counting sort, steps 1-2: bucket offsets = exclusive scan of the counts, over kSortBins / 1024
@@ -570,12 +607,15 @@ cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_g
   using WT = std::integral_constant<bool, true>;
   using MT = std::integral_constant<bool, false>;
   using Bin = std::integral_constant<int, kWalkBinary>;
+  using Cnt = std::integral_constant<int, kWalkCount>;
   using Wide = std::integral_constant<int, kWalkWide>;
   if (l.watertight) {
-    if (l.wide) go(WT{}, Wide{});
+    if (l.count) go(WT{}, Cnt{});
+    else if (l.wide) go(WT{}, Wide{});
     else go(WT{}, Bin{});
   } else {
-    if (l.wide) go(MT{}, Wide{});
+    if (l.count) go(MT{}, Cnt{});
+    else if (l.wide) go(MT{}, Wide{});
     else go(MT{}, Bin{});
   }
   k_wf_control<<<1, 1, 0, st>>>(dparams, use_graph ? 1 : 0);
@@ -587,10 +627,11 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, int blocks_per_sm_cap) {
+WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap) {
   WfLaunch l{};
   l.watertight = watertight;
   l.wide = wide;
+  l.count = count;
   l.sort = sort;
   l.sort_shadow = sort && sort_shadow;
   auto cap = [&](int g) {
@@ -611,12 +652,15 @@ WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow
   using WT = std::integral_constant<bool, true>;
   using MT = std::integral_constant<bool, false>;
   using Bin = std::integral_constant<int, kWalkBinary>;
+  using Cnt = std::integral_constant<int, kWalkCount>;
   using Wide = std::integral_constant<int, kWalkWide>;
   if (watertight) {
-    if (wide) shape(WT{}, Wide{});
+    if (count) shape(WT{}, Cnt{});
+    else if (wide) shape(WT{}, Wide{});
     else shape(WT{}, Bin{});
   } else {
-    if (wide) shape(MT{}, Wide{});
+    if (count) shape(MT{}, Cnt{});
+    else if (wide) shape(MT{}, Wide{});
     else shape(MT{}, Bin{});
   }
   return l;

@@ -59,6 +59,7 @@ struct WfParams {
   unsigned* off;                // kSortBins bucket offsets, then kSortBins / 1024 tile sums
   float4* shadow;               // 4 float4 per record: (o, tmax), (d, owner), a, b
   int* counters;                // kCntSize ints
+  void* trace_counters;         // DevCounters (rays, nodes, triangles, instances) of counting walks
   unsigned long long* work_next;
   double* film_acc;             // 3 doubles per pixel
   float* film_out;              // 3 floats per pixel
@@ -70,9 +71,10 @@ struct WfLaunch {
   bool watertight;
   bool wide;                    // the scene's wide records (kWalkWide kernels)
   bool sort, sort_shadow;       // ray / shadow queue sorted by ray key before extend / shadow
+  bool count;                   // binary walks that count their visits (BN_RENDER_COUNT)
 };
 
-WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, int blocks_per_sm_cap);
+WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap);
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
 cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st);
 

@@ -310,12 +310,15 @@ def main():
     torch.cuda.set_device(dev)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
 
-    # algorithmic bytes per launch of the dominant kernel: an instrumented run of one step
+    primary = capi.BN_MODE_WAVEFRONT if args.mode == "wavefront" else capi.BN_MODE_MEGAKERNEL
+    # algorithmic bytes per launch of the dominant kernel: an instrumented run of one step in the
+    # timed form (the wavefront does not trace shadow rays that cannot change the radiance, so its
+    # rays are counted on its own walk), visits counted in the reference's binary traversal order
     rc = capi.bn_render_desc()
     C_copy = bytes(r)
     C.memmove(C.addressof(rc), C_copy, len(C_copy))
     rc.flags |= capi.BN_RENDER_COUNT
-    rc.mode = capi.BN_MODE_MEGAKERNEL  # both forms trace the same rays; the megakernel counts them
+    rc.mode = primary
     rc.frame_id = 100
     ctx.reset_stats()
     ctx.render(rc, views, to_host=False)
@@ -347,7 +350,6 @@ def main():
         barrier(dist)
         return max_over_ranks(dist, dev_ms / 1000.0), dom_ms, launches, wall
 
-    primary = capi.BN_MODE_WAVEFRONT if args.mode == "wavefront" else capi.BN_MODE_MEGAKERNEL
     other = capi.BN_MODE_MEGAKERNEL if primary == capi.BN_MODE_WAVEFRONT else capi.BN_MODE_WAVEFRONT
     with ClockSampler(dev) as clk:
         dev_s, dom_ms, launches, wall = timed(primary, 0)

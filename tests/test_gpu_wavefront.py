@@ -92,3 +92,24 @@ def test_wavefront_watertight_and_depth_zero(ctx):
     r.max_depth = 0
     r.mode = capi.BN_MODE_WAVEFRONT
     assert np.all(ctx.render(r, [v])[0] == 0)
+
+
+def test_wavefront_counting_render_and_shadow_culling(ctx):
+    """A counting render walks the binary tree in the reference's order and gives the same image;
+    the wavefront traces the megakernel's closest-hit rays but no shadow ray whose contribution is
+    exactly zero, so it counts fewer rays than the megakernel on the same paths."""
+    b = Bundle.generate("cornell-objects", 1)
+    ctx.upload(b)
+    v = b.views
+    plain = render(ctx, b, v, 2, capi.BN_MODE_WAVEFRONT)[0]
+    counts = {}
+    for mode in (capi.BN_MODE_WAVEFRONT, capi.BN_MODE_MEGAKERNEL):
+        ctx.reset_stats()
+        img = render(ctx, b, v, 2, mode, flags=capi.BN_RENDER_COUNT)[0]
+        st = ctx.stats()
+        counts[mode] = (st.rays, st.nodes_visited, st.tris_tested, st.instances_visited)
+        assert_same_image(img, plain)
+    wf, mk = counts[capi.BN_MODE_WAVEFRONT], counts[capi.BN_MODE_MEGAKERNEL]
+    assert 0 < wf[0] < mk[0] and 0 < wf[1] < mk[1]
+    # every path's camera ray is traced by both
+    assert wf[0] > v[0].width * v[0].height * 2
