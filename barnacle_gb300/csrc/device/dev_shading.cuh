@@ -396,6 +396,18 @@ struct PathCounters {
   TraceCounters tc;
 };
 
+// A light sample adds fma(a, b, L) per channel when its shadow ray is unoccluded (a = beta * f,
+// b = L_e / pdf).  Where every a*b is exactly zero (a factor 0 and the other finite) and L holds
+// no -0, that leaves L's bits as they are, so the shadow ray need not be traced: light samples
+// below the shading point's horizon (f = 0) and the back of one-sided lights (L_e = 0).
+__device__ __forceinline__ bool shadow_contributes(V3 a, V3 b, V3 L) {
+  auto zero = [](float x, float y, float l) {
+    const bool prod0 = (x == 0.f && isfinite(y)) || (y == 0.f && isfinite(x));
+    return prod0 && !(l == 0.f && signbit(l));
+  };
+  return !(zero(a.x, b.x, L.x) && zero(a.y, b.y, L.y) && zero(a.z, b.z, L.z));
+}
+
 // The state of one path between bounces (PathTracingIntegrator.Li's loop variables).
 struct PathState {
   Ray ray;
@@ -418,7 +430,10 @@ __device__ __forceinline__ void path_begin(PathState& ps, const Ray& ray) {
 // Draw order per bounce: u_select, u_light.xy (NEE), u_lobe, u_bsdf.xy, then u_rr if depth >=
 // rr_depth (PathTracing) / always (PSSMLT).  Reciprocal estimates are exact reciprocals here.
 // kOutline: one out-of-line walk for both queries (see trace_walk_outline).
-template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false>
+// kCull: evaluate the light sample first and trace its shadow ray only if it can contribute
+// (shadow_contributes); the result is the same, the plain megakernel keeps the reference's order.
+template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false,
+          bool kCull = false>
 __device__ __forceinline__ bool li_bounce(const DevScene& s, PathState& ps, Smp& smp, int max_depth, int rr_depth,
                                           PathCounters* pc) {
   constexpr bool kCount = kWalk == kWalkCount;
@@ -452,10 +467,19 @@ __device__ __forceinline__ bool li_bounce(const DevScene& s, PathState& ps, Smp&
     Ray sh;
     sh.o = it.p;
     sh.d = ls.wi;
-    if (kCount) pc->rays++;
-    if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
+    if (kCull) {
       const BsdfEval be = bsdf_eval<kSimple>(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
-      ps.L = fma3(mul(ps.beta, be.f), scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L), ps.L);
+      const V3 a = mul(ps.beta, be.f), b = scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L);
+      if (shadow_contributes(a, b, ps.L)) {
+        if (kCount) pc->rays++;
+        if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) ps.L = fma3(a, b, ps.L);
+      }
+    } else {
+      if (kCount) pc->rays++;
+      if (!trace_any<kWT, kWalk, kOutline>(s, sh, __fsub_rn(dist, 1e-3f), &pc->tc)) {
+        const BsdfEval be = bsdf_eval<kSimple>(m, to_local(it.f, wo_w), to_local(it.f, ls.wi));
+        ps.L = fma3(mul(ps.beta, be.f), scale(__frcp_rn(__fadd_rn(be.pdf, ls.pdf)), ls.L), ps.L);
+      }
     }
   }
   if (!kFixed7) { u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); }
@@ -476,11 +500,12 @@ __device__ __forceinline__ bool li_bounce(const DevScene& s, PathState& ps, Smp&
 }
 
 // the whole path: PathTracingIntegrator.Li / PSSMLTIntegrator.Li
-template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false>
+template <bool kWT, bool kFixed7, int kWalk, class Smp, bool kOutline = false, bool kSimple = false,
+          bool kCull = false>
 __device__ __forceinline__ V3 li_path(const DevScene& s, Ray ray, Smp& smp, int max_depth, int rr_depth, PathCounters* pc) {
   PathState ps;
   path_begin(ps, ray);
-  while (!li_bounce<kWT, kFixed7, kWalk, Smp, kOutline, kSimple>(s, ps, smp, max_depth, rr_depth, pc)) {
+  while (!li_bounce<kWT, kFixed7, kWalk, Smp, kOutline, kSimple, kCull>(s, ps, smp, max_depth, rr_depth, pc)) {
   }
   return ps.L;
 }

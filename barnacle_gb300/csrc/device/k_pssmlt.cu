@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(128) k_mlt_bootstrap(MltParams p) {
   int x, y;
   const Ray ray = mlt_camera(*p.view, smp, &x, &y);
   PathCounters pc{};
-  const V3 L = li_path<kWT, true, kWalk>(p.scene, ray, smp, p.max_depth, p.rr_depth, &pc);
+  const V3 L = li_path<kWT, true, kWalk, IndepSampler, false, false, true>(p.scene, ray, smp, p.max_depth, p.rr_depth, &pc);
   p.weights[id] = luminance(L);
 }
 
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
       m.start_iteration();
       int nx, ny;
       const Ray ray = mlt_camera(v, m, &nx, &ny);
-      const V3 Ln = li_path<kWT, true, kWalk>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
+      const V3 Ln = li_path<kWT, true, kWalk, MltSampler, false, false, true>(p.scene, ray, m, p.max_depth, p.rr_depth, &pc);
       const float yn = luminance(Ln);
       if (it < 0) {
         L = Ln;

@@ -237,18 +237,6 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
   if (kWalk == kWalkCount) add_trace_counts(p.trace_counters, nrays, tc);
 }
 
-// The shadow kernel adds fma(a, b, L) per channel when the shadow ray is unoccluded.  Where every
-// a*b is exactly zero (a factor 0 and the other finite) and L holds no -0, that leaves L as it is,
-// so the ray need not be queued: below-horizon light samples (f = 0) and the back of one-sided
-// lights (L_e = 0) cost no traversal, and the path's radiance keeps the same bits.
-__device__ __forceinline__ bool shadow_contributes(V3 a, V3 b, V3 L) {
-  auto zero = [](float x, float y, float l) {
-    const bool prod0 = (x == 0.f && isfinite(y)) || (y == 0.f && isfinite(x));
-    return prod0 && !(l == 0.f && signbit(l));
-  };
-  return !(zero(a.x, b.x, L.x) && zero(a.y, b.y, L.y) && zero(a.z, b.z, L.z));
-}
-
 // DirectIntegrator.Li (Extensions/Integrator/Direct.fs:10-40) as two wavefront vertices.  At the
 // camera hit: emission seen directly (EvalEmit(-d)), a shadow record for one light sample (a = f,
 // b = L_light / pdf_light; the shadow kernel adds fma(a, b, L) if unoccluded, as the reference's
