@@ -231,13 +231,13 @@ __device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, 
   return kStepOk;
 }
 
-// one step (a node pair, one instance, and one triangle (kFine) or the rest of a leaf's
-// triangles); returns true once the walk is finished (tr.found / tr.hit hold the answer).
-// kFine suits lanes that are refilled with new rays; a single-ray walk runs fewer, coarser steps.
+// one step (a node record or pair, one instance, or kTris triangles of a leaf, 0 = the rest of
+// it); returns true once the walk is finished (tr.found / tr.hit hold the answer).  Small steps
+// suit lanes that are refilled with new rays; a single-ray walk runs fewer, coarser steps.
 // kAny: kClosest, kAnyHit, or kAnyRuntime (tr.any decides).  Every branch that exhausts its unit
 // asks for a pop, which runs once at the end of the step.
 enum : int { kClosest = 0, kAnyHit = 1, kAnyRuntime = 2 };
-template <int kAny, bool kWT, int kWalk, bool kFine = true>
+template <int kAny, bool kWT, int kWalk, int kTris = 1>
 __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, float* st, TraceCounters* cnt) {
   constexpr bool kCount = kWalk == kWalkCount, kWide = kWalk == kWalkWide;
   const bool any = kAny == kAnyRuntime ? tr.any : kAny == kAnyHit;
@@ -277,7 +277,9 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
       pop = true;
     }
   } else if (tr.mode == kTravTri) {
-    // one triangle of a BLAS leaf: its AABB pre-test (Mesh.fs:204,231), then the triangle test
+    // kTris triangles of a BLAS leaf (0: the rest of the leaf): each its AABB pre-test
+    // (Mesh.fs:204,231), then the triangle test
+    int done = 0;
 #pragma unroll 1
     while (tr.ti < tr.ti_end) {
       const int j = tr.ti++;
@@ -300,7 +302,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
           tr.hit.inst = tr.inst; tr.hit.tri = j; tr.hit.t = tt; tr.hit.u = uu; tr.hit.v = vv; tr.hit.sphere_root = 0;
         }
       }
-      if (kFine) break;
+      if (kTris > 0 && ++done >= kTris) break;
     }
     pop = tr.ti >= tr.ti_end;
   } else if (tr.mode == kTravInst) {
@@ -381,7 +383,7 @@ __device__ __forceinline__ bool trace_walk_inline(const DevScene& s, const Ray& 
   float st[kStackSize];
   Trav tr;
   trav_init<kWalk>(tr, s, ray, tmax, cnt);
-  while (!trav_step<kAny, kWT, kWalk, false>(tr, s, sn, st, cnt)) {
+  while (!trav_step<kAny, kWT, kWalk, 0>(tr, s, sn, st, cnt)) {
   }
   if (kAny == kClosest) *hit = tr.hit;
   return tr.found;
@@ -399,7 +401,7 @@ __device__ __noinline__ bool trace_walk_outline(const DevScene& s, const Ray& ra
   Trav tr;
   tr.any = any;
   trav_init<kWalk>(tr, s, ray, tmax, cnt);
-  while (!trav_step<kAnyRuntime, kWT, kWalk, false>(tr, s, sn, st, cnt)) {
+  while (!trav_step<kAnyRuntime, kWT, kWalk, 0>(tr, s, sn, st, cnt)) {
   }
   if (!any) *hit = tr.hit;
   return tr.found;
