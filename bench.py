@@ -381,6 +381,14 @@ def main():
             if line.startswith("bytes_per_launch:"):
                 # measured at the default 4 spp per step; other step sizes report none
                 traffic = int(line.split(":")[1]) if args.spp_per_step == 4 else None
+    l2 = None  # the L2 side of the roofline, from the ncu summary of the dominant kernel
+    prof = ROOT / "profiles" / ("k_pt_mega_instances.md" if args.mode == "megakernel" else "k_wf_extend_instances.md")
+    if args.workload == "instances" and prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("l2:"):
+                kv = dict(f.split("=") for f in line[3:].split())
+                l2 = {"kernel": kv["kernel"], "hit_rate": float(kv["hit_rate"]),
+                      "throughput_frac": float(kv["throughput_frac"]), "source": f"profiles/{prof.name} (ncu)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -412,7 +420,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_pt_mega" if args.mode == "megakernel" else
                                    "wavefront bounce loop (regen+extend+shade+shadow, one graph)",
-                         "alg_bytes_per_launch": int(alg_bytes)},
+                         "alg_bytes_per_launch": int(alg_bytes), "l2": l2},
             "cpu_baseline": cpu,
             "e2e": {"value": world * paths_per_step * args.steps / e2e_s, "unit": "paths/s",
                     "h2d_bytes_per_step": C.sizeof(capi.bn_view) * len(views),
