@@ -142,10 +142,10 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.frame_id = d->frame_id;
   p.integrator = d->integrator;
   p.pool = pool;
-  // refill thresholds (lanes of 32 still walking), measured on the 1,024-instance workload: 16-24
-  // are within 0.5% of each other; 31 (refill as soon as one lane is free) is 19% slower, 0 11%
-  p.refill_extend = 20;
-  p.refill_shadow = 20;
+  // refill thresholds (lanes of 32 still walking), measured on the 1,024-instance workload with
+  // the mode vote: 12 / 16 / 20 / 24 / 28 give 192.9 / 193.7 / 191.6 / 187.8 / 179.5 M paths/s
+  p.refill_extend = 16;
+  p.refill_shadow = 16;
   p.total_paths = total_paths;
   p.n_pixels = n_pixels;
   p.max_iters = static_cast<int>(std::min<long long>(1LL << 30, (total_paths / pool + 2) * (d->max_depth + 2) + 64));

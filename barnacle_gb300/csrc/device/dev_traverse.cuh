@@ -231,13 +231,13 @@ __device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, 
   return kStepOk;
 }
 
-// one step (a node record or pair, one instance, or kTris triangles of a leaf, 0 = the rest of
-// it); returns true once the walk is finished (tr.found / tr.hit hold the answer).  Small steps
-// suit lanes that are refilled with new rays; a single-ray walk runs fewer, coarser steps.
+// one step: a wide record or a node pair, one instance (kInstRun: the leaf's instances until one
+// is entered), or kTris triangles of a leaf (0 = the rest of it); returns true once the walk is
+// finished (tr.found / tr.hit hold the answer).
 // kAny: kClosest, kAnyHit, or kAnyRuntime (tr.any decides).  Every branch that exhausts its unit
 // asks for a pop, which runs once at the end of the step.
 enum : int { kClosest = 0, kAnyHit = 1, kAnyRuntime = 2 };
-template <int kAny, bool kWT, int kWalk, int kTris = 1>
+template <int kAny, bool kWT, int kWalk, int kTris = 1, bool kInstRun = false>
 __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, float* st, TraceCounters* cnt) {
   constexpr bool kCount = kWalk == kWalkCount, kWide = kWalk == kWalkWide;
   const bool any = kAny == kAnyRuntime ? tr.any : kAny == kAnyHit;
@@ -306,9 +306,11 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     }
     pop = tr.ti >= tr.ti_end;
   } else if (tr.mode == kTravInst) {
-    // one instance of a TLAS leaf (PrimitiveInstance.Intersect, Primitive.fs:111-129)
+    // the next instance of a TLAS leaf, or with kInstRun the leaf's instances until one is
+    // entered (PrimitiveInstance.Intersect, Primitive.fs:111-129)
     bool entered = false;
-    if (tr.ii < tr.ii_end) {
+#pragma unroll 1
+    while (!entered && tr.ii < tr.ii_end) {
       const int k = tr.ii++;
       const DevInstance* I = s.inst + k;
       if (kCount) cnt->insts++;
@@ -368,11 +370,27 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
           }
         }
       }
+      if (!kInstRun) break;
     }
     pop = !entered && tr.ii >= tr.ii_end;
   }
   if (pop) trav_pop<kWide>(tr, s, sn, st);
   return tr.mode == kTravDone;
+}
+
+// Lanes of a warp at different kinds of unit (a node record, a leaf's triangles, instances) run
+// different branches of a step one after the other, each with its own chain of dependent loads.
+// With this vote only the lanes in the mode with the largest weighted count take the step
+// (instances weigh 3, nodes and triangles 2); the others keep their state and wait.  Each lane's
+// sequence of units is unchanged, so its result is too.  Call it with every lane of the warp
+// that is in the loop; walking = the lane holds a walk that is not finished.
+__device__ __forceinline__ bool trav_vote(bool walking, int mode) {
+  const unsigned act = __activemask();
+  const int cn = 2 * __popc(__ballot_sync(act, walking && mode == kTravNode));
+  const int ct = 2 * __popc(__ballot_sync(act, walking && mode == kTravTri));
+  const int ci = 3 * __popc(__ballot_sync(act, walking && mode == kTravInst));
+  const int pick = (cn >= ct && cn >= ci) ? kTravNode : (ct >= ci ? kTravTri : kTravInst);
+  return mode == pick || mode == kTravDone;
 }
 
 // A walk, inlined at its call site with the query fixed at compile time.

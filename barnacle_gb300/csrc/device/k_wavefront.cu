@@ -27,9 +27,11 @@ namespace {
 
 constexpr int kStatusFree = 0, kStatusActive = 1, kStatusDone = 2;
 constexpr int kBinMiss = 4, kBinNoMaterial = 5;
-// triangles a lane tests per traversal step (the lanes of a warp step together, so a leaf's
-// remaining triangles wait for the slowest lane)
-constexpr int kWfTris = 1;
+// the wavefront's traversal step: one wide record, a whole BLAS leaf (at most 4 triangles), or a
+// TLAS leaf's instances until one is entered; only the lanes that win the mode vote (trav_vote)
+// take it
+constexpr int kWfTris = 4;
+constexpr bool kWfInstRun = true;
 
 __device__ __forceinline__ int warp_append(int* counter, bool pred) {
   // ballot + popc compaction: one atomic per warp
@@ -232,7 +234,8 @@ __global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict
       }
     }
     // a walk can end at init (root box missed)
-    if (have && (tr.mode == kTravDone || trav_step<kClosest, kWT, kWalk, kWfTris>(tr, s, sn, st, &tc))) {
+    const bool go = trav_vote(have, tr.mode);
+    if (have && go && (tr.mode == kTravDone || trav_step<kClosest, kWT, kWalk, kWfTris, kWfInstRun>(tr, s, sn, st, &tc))) {
       have = false;
       pending = true;
     }
@@ -455,7 +458,8 @@ __global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict
         ++nrays;
       }
     }
-    if (have && (tr.mode == kTravDone || trav_step<kAnyHit, kWT, kWalk, kWfTris>(tr, p.scene, sn, st, &tc))) {
+    const bool go = trav_vote(have, tr.mode);
+    if (have && go && (tr.mode == kTravDone || trav_step<kAnyHit, kWT, kWalk, kWfTris, kWfInstRun>(tr, p.scene, sn, st, &tc))) {
       have = false;
       pending = true;
     }
