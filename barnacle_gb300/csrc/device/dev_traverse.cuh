@@ -385,10 +385,13 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
 // sequence of units is unchanged, so its result is too.  Call it with every lane of the warp
 // that is in the loop; walking = the lane holds a walk that is not finished.
 __device__ __forceinline__ bool trav_vote(bool walking, int mode) {
+  static_assert(kTravNode == 0 && kTravTri == 1 && kTravInst == 2 && kTravDone == 3, "mode bits");
+  // two ballots on the mode's bits; a lane that is not walking counts as done (both bits)
   const unsigned act = __activemask();
-  const int cn = 2 * __popc(__ballot_sync(act, walking && mode == kTravNode));
-  const int ct = 2 * __popc(__ballot_sync(act, walking && mode == kTravTri));
-  const int ci = 3 * __popc(__ballot_sync(act, walking && mode == kTravInst));
+  const unsigned b0 = __ballot_sync(act, !walking || (mode & 1)), b1 = __ballot_sync(act, !walking || (mode & 2));
+  const int cn = 2 * __popc(act & ~(b0 | b1));
+  const int ct = 2 * __popc(b0 & ~b1);
+  const int ci = 3 * __popc(b1 & ~b0);
   const int pick = (cn >= ct && cn >= ci) ? kTravNode : (ct >= ci ? kTravTri : kTravInst);
   return mode == pick || mode == kTravDone;
 }

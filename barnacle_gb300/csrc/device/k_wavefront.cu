@@ -32,6 +32,8 @@ constexpr int kBinMiss = 4, kBinNoMaterial = 5;
 // take it
 constexpr int kWfTris = 4;
 constexpr bool kWfInstRun = true;
+// blocks of 128 per SM the traversal kernels are compiled for (registers: 65,536 / (128 x blocks))
+constexpr int kExtendBlocks = 7, kShadowBlocks = 8;
 
 __device__ __forceinline__ int warp_append(int* counter, bool pred) {
   // ballot + popc compaction: one atomic per warp
@@ -179,7 +181,7 @@ __device__ __forceinline__ int fetch_next(int* counter, bool need) {
 }
 
 template <bool kWT, int kWalk>
-__global__ void __launch_bounds__(128, 7) k_wf_extend(const WfParams* __restrict__ pp) {
+__global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
   const int n = p.counters[kCntActive];
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
 }
 
 template <bool kWT, int kWalk>
-__global__ void __launch_bounds__(128, 8) k_wf_shadow(const WfParams* __restrict__ pp) {
+__global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
   const int refill_below = p.refill_shadow;
