@@ -100,6 +100,44 @@ __device__ __forceinline__ void trav_enter_leaf(Trav& tr, int first, int count) 
   }
 }
 
+// The walk's stack of far entries: a node or record index (or a leaf slot) with its entry
+// distance.  LocalStack keeps them in the thread's local memory.  SharedStack keeps the bottom
+// kShared entries in shared memory, one column per thread of a kBlock-thread block (lanes at
+// different depths then fall on different banks), and the deeper ones in local memory, so the
+// pushes and pops of a typical walk stay out of the L1 data cache the node loads use.
+struct LocalStack {
+  int sn[kStackSize];
+  float st[kStackSize];
+  __device__ __forceinline__ void put(int i, int n, float t) { sn[i] = n; st[i] = t; }
+  __device__ __forceinline__ void get(int i, int* n, float* t) const { *n = sn[i]; *t = st[i]; }
+};
+
+template <int kShared, int kBlock>
+struct SharedStack {
+  int2* col;  // this thread's column of the block's kShared x kBlock array
+  int sn[kStackSize - kShared];
+  float st[kStackSize - kShared];
+  __device__ __forceinline__ explicit SharedStack(int2* block_array) : col(block_array + threadIdx.x) {}
+  __device__ __forceinline__ void put(int i, int n, float t) {
+    if (i < kShared) {
+      col[i * kBlock] = make_int2(n, __float_as_int(t));
+    } else {
+      sn[i - kShared] = n;
+      st[i - kShared] = t;
+    }
+  }
+  __device__ __forceinline__ void get(int i, int* n, float* t) const {
+    if (i < kShared) {
+      const int2 e = col[i * kBlock];
+      *n = e.x;
+      *t = __int_as_float(e.y);
+    } else {
+      *n = sn[i - kShared];
+      *t = st[i - kShared];
+    }
+  }
+};
+
 __device__ __forceinline__ const float4* node4_at(const DevScene& s, int i) {
   return s.nodes4 + 8 * static_cast<size_t>(i);
 }
@@ -107,14 +145,16 @@ __device__ __forceinline__ const float4* node4_at(const DevScene& s, int i) {
 // the next stacked node still within reach; an exhausted BLAS returns to the instances of its
 // TLAS leaf, an exhausted TLAS ends the walk.  Binary entries are node indices within the level;
 // wide entries are record indices (>= 0) or -1 - (4 * record + slot) for a leaf slot.
-template <bool kWide>
-__device__ __forceinline__ void trav_pop(Trav& tr, const DevScene& s, const int* sn, const float* st) {
+template <bool kWide, class Stack>
+__device__ __forceinline__ void trav_pop(Trav& tr, const DevScene& s, const Stack& stk) {
   for (;;) {
     const int bottom = tr.level ? tr.blas_sp0 : 0;
     while (tr.sp > bottom) {
       --tr.sp;
-      if (st[tr.sp] <= tr.t) {
-        const int c = sn[tr.sp];
+      int c;
+      float te;
+      stk.get(tr.sp, &c, &te);
+      if (te <= tr.t) {
         if (!kWide) {
           trav_enter(tr, c, load_node(s.nodes, tr.base + c));
         } else if (c >= 0) {
@@ -182,7 +222,8 @@ __device__ __forceinline__ int sel4(int a, int b, int c, int d, int i) {
 // one wide step: the four slot boxes of record tr.cur; returns kStepPop when none is entered,
 // kStepOverflow when the stack is full
 enum : int { kStepOk = 0, kStepPop = 1, kStepOverflow = 2 };
-__device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, float* st) {
+template <class Stack>
+__device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, Stack& stk) {
   const Ray& r = tr.level ? tr.orr : tr.wr;
   const V3 inv = tr.level ? tr.oinv : tr.winv;
   const float4* q = node4_at(s, tr.cur);
@@ -219,8 +260,8 @@ __device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, 
   for (int k = 3; k >= 1; --k) {
     const int sl = v[k];
     if (k > first && ((hm >> sl) & 1)) {
-      sn[tr.sp] = ((m >> sl) & 1) ? -1 - (4 * tr.cur + sl) : sel4(ref.x, ref.y, ref.z, ref.w, sl);
-      st[tr.sp] = sel4(e0, e1, e2, e3, sl);
+      stk.put(tr.sp, ((m >> sl) & 1) ? -1 - (4 * tr.cur + sl) : sel4(ref.x, ref.y, ref.z, ref.w, sl),
+              sel4(e0, e1, e2, e3, sl));
       ++tr.sp;
     }
   }
@@ -237,13 +278,13 @@ __device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, int* sn, 
 // kAny: kClosest, kAnyHit, or kAnyRuntime (tr.any decides).  Every branch that exhausts its unit
 // asks for a pop, which runs once at the end of the step.
 enum : int { kClosest = 0, kAnyHit = 1, kAnyRuntime = 2 };
-template <int kAny, bool kWT, int kWalk, int kTris = 1, bool kInstRun = false>
-__device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, float* st, TraceCounters* cnt) {
+template <int kAny, bool kWT, int kWalk, int kTris = 1, bool kInstRun = false, class Stack>
+__device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, Stack& stk, TraceCounters* cnt) {
   constexpr bool kCount = kWalk == kWalkCount, kWide = kWalk == kWalkWide;
   const bool any = kAny == kAnyRuntime ? tr.any : kAny == kAnyHit;
   bool pop = false;
   if (kWide && tr.mode == kTravNode) {
-    const int r = trav_node4(tr, s, sn, st);
+    const int r = trav_node4(tr, s, stk);
     if (r == kStepOverflow) {
       flag_error(s, BN_DEVERR_STACK_OVERFLOW);
       tr.mode = kTravDone;
@@ -267,8 +308,8 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
         tr.mode = kTravDone;
         return true;
       }
-      if (left_first) { sn[tr.sp] = ri; st[tr.sp] = tb; ++tr.sp; trav_enter(tr, li, a); }
-      else { sn[tr.sp] = li; st[tr.sp] = ta; ++tr.sp; trav_enter(tr, ri, b); }
+      if (left_first) { stk.put(tr.sp, ri, tb); ++tr.sp; trav_enter(tr, li, a); }
+      else { stk.put(tr.sp, li, ta); ++tr.sp; trav_enter(tr, ri, b); }
     } else if (ha) {
       trav_enter(tr, li, a);
     } else if (hb) {
@@ -374,7 +415,7 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, int* sn, 
     }
     pop = !entered && tr.ii >= tr.ii_end;
   }
-  if (pop) trav_pop<kWide>(tr, s, sn, st);
+  if (pop) trav_pop<kWide>(tr, s, stk);
   return tr.mode == kTravDone;
 }
 
@@ -400,11 +441,10 @@ __device__ __forceinline__ bool trav_vote(bool walking, int mode) {
 template <int kAny, bool kWT, int kWalk>
 __device__ __forceinline__ bool trace_walk_inline(const DevScene& s, const Ray& ray, float tmax, HitRec* hit,
                                                   TraceCounters* cnt) {
-  int sn[kStackSize];
-  float st[kStackSize];
+  LocalStack stk;
   Trav tr;
   trav_init<kWalk>(tr, s, ray, tmax, cnt);
-  while (!trav_step<kAny, kWT, kWalk, 0>(tr, s, sn, st, cnt)) {
+  while (!trav_step<kAny, kWT, kWalk, 0>(tr, s, stk, cnt)) {
   }
   if (kAny == kClosest) *hit = tr.hit;
   return tr.found;
@@ -417,12 +457,11 @@ __device__ __forceinline__ bool trace_walk_inline(const DevScene& s, const Ray& 
 template <bool kWT, int kWalk>
 __device__ __noinline__ bool trace_walk_outline(const DevScene& s, const Ray& ray, float tmax, bool any, HitRec* hit,
                                                 TraceCounters* cnt) {
-  int sn[kStackSize];
-  float st[kStackSize];
+  LocalStack stk;
   Trav tr;
   tr.any = any;
   trav_init<kWalk>(tr, s, ray, tmax, cnt);
-  while (!trav_step<kAnyRuntime, kWT, kWalk, 0>(tr, s, sn, st, cnt)) {
+  while (!trav_step<kAnyRuntime, kWT, kWalk, 0>(tr, s, stk, cnt)) {
   }
   if (!any) *hit = tr.hit;
   return tr.found;

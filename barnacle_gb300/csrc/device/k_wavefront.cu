@@ -34,6 +34,9 @@ constexpr int kWfTris = 4;
 constexpr bool kWfInstRun = true;
 // blocks of 128 per SM the traversal kernels are compiled for (registers: 65,536 / (128 x blocks))
 constexpr int kExtendBlocks = 7, kShadowBlocks = 8;
+// stack entries per lane kept in shared memory (8 bytes each, x 128 lanes per block)
+constexpr int kWfSharedStack = 16;
+using WfStack = SharedStack<kWfSharedStack, 128>;
 
 __device__ __forceinline__ int warp_append(int* counter, bool pred) {
   // ballot + popc compaction: one atomic per warp
@@ -186,8 +189,8 @@ __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams
   const DevScene& s = p.scene;
   const int n = p.counters[kCntActive];
   const int refill_below = p.refill_extend;
-  int sn[kStackSize];
-  float st[kStackSize];
+  __shared__ int2 stack_block[kWfSharedStack * 128];
+  WfStack stk(stack_block);
   Trav tr;
   TraceCounters tc{0, 0, 0};
   unsigned long long nrays = 0;  // rays this lane walked (counting walks)
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams
     }
     // a walk can end at init (root box missed)
     const bool go = trav_vote(have, tr.mode);
-    if (have && go && (tr.mode == kTravDone || trav_step<kClosest, kWT, kWalk, kWfTris, kWfInstRun>(tr, s, sn, st, &tc))) {
+    if (have && go && (tr.mode == kTravDone || trav_step<kClosest, kWT, kWalk, kWfTris, kWfInstRun>(tr, s, stk, &tc))) {
       have = false;
       pending = true;
     }
@@ -424,8 +427,8 @@ __global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
   const int refill_below = p.refill_shadow;
-  int sn[kStackSize];
-  float st[kStackSize];
+  __shared__ int2 stack_block[kWfSharedStack * 128];
+  WfStack stk(stack_block);
   Trav tr;
   TraceCounters tc{0, 0, 0};
   unsigned long long nrays = 0;  // rays this lane walked (counting walks)
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams
       }
     }
     const bool go = trav_vote(have, tr.mode);
-    if (have && go && (tr.mode == kTravDone || trav_step<kAnyHit, kWT, kWalk, kWfTris, kWfInstRun>(tr, p.scene, sn, st, &tc))) {
+    if (have && go && (tr.mode == kTravDone || trav_step<kAnyHit, kWT, kWalk, kWfTris, kWfInstRun>(tr, p.scene, stk, &tc))) {
       have = false;
       pending = true;
     }
