@@ -13,7 +13,7 @@ namespace {
 
 struct WfState {
   int pool = 0;
-  DevBuf params, ray_o, ray_d, beta, L, meta, hit_f, hit_i, q_active, q_bins, shadow, counters, work_next, film_acc;
+  DevBuf params, ray, bl, hit, meta, q_active, q_bins, shadow, counters, work_next, film_acc;
   DevBuf slot_key, q_key, q_ray, sh_key, q_shadow, hist, off;
   // captured graph (one per launch shape)
   cudaGraph_t graph = nullptr;
@@ -28,7 +28,7 @@ struct WfState {
   int tuned_pool = 0, tuned_cap = 0;
 
   void release() {
-    DevBuf* b[] = {&params, &ray_o, &ray_d, &beta, &L, &meta, &hit_f, &hit_i, &q_active, &q_bins, &shadow, &counters,
+    DevBuf* b[] = {&params, &ray, &bl, &hit, &meta, &q_active, &q_bins, &shadow, &counters,
                    &work_next, &film_acc, &slot_key, &q_key, &q_ray, &sh_key, &q_shadow, &hist, &off};
     for (DevBuf* x : b) x->release();
     if (exec) cudaGraphExecDestroy(exec);
@@ -55,13 +55,10 @@ cudaError_t ensure_pool(WfState* w, int pool) {
   cudaError_t e;
   const size_t P = static_cast<size_t>(pool);
   if ((e = w->params.reserve(sizeof(bn::WfParams))) != cudaSuccess) return e;
-  if ((e = w->ray_o.reserve(P * sizeof(float4))) != cudaSuccess) return e;
-  if ((e = w->ray_d.reserve(P * sizeof(float4))) != cudaSuccess) return e;
-  if ((e = w->beta.reserve(P * sizeof(float4))) != cudaSuccess) return e;
-  if ((e = w->L.reserve(P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->ray.reserve(2 * P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->bl.reserve(2 * P * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = w->hit.reserve(2 * P * sizeof(float4))) != cudaSuccess) return e;
   if ((e = w->meta.reserve(P * sizeof(int4))) != cudaSuccess) return e;
-  if ((e = w->hit_f.reserve(P * sizeof(float4))) != cudaSuccess) return e;
-  if ((e = w->hit_i.reserve(P * sizeof(int2))) != cudaSuccess) return e;
   if ((e = w->q_active.reserve(P * sizeof(int))) != cudaSuccess) return e;
   if ((e = w->q_bins.reserve(P * bn::kNumBins * sizeof(int))) != cudaSuccess) return e;
   if ((e = w->shadow.reserve(P * 4 * sizeof(float4))) != cudaSuccess) return e;
@@ -149,13 +146,10 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.total_paths = total_paths;
   p.n_pixels = n_pixels;
   p.max_iters = static_cast<int>(std::min<long long>(1LL << 30, (total_paths / pool + 2) * (d->max_depth + 2) + 64));
-  p.ray_o = w->ray_o.as<float4>();
-  p.ray_d = w->ray_d.as<float4>();
-  p.beta = w->beta.as<float4>();
-  p.L = w->L.as<float4>();
+  p.ray = w->ray.as<float4>();
+  p.bl = w->bl.as<float4>();
+  p.hit = w->hit.as<float4>();
   p.meta = w->meta.as<int4>();
-  p.hit_f = w->hit_f.as<float4>();
-  p.hit_i = w->hit_i.as<int2>();
   p.q_active = w->q_active.as<int>();
   p.sort = sort ? 1 : 0;
   p.sort_shadow = sort_shadow ? 1 : 0;

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
     const bool valid = slot < p.pool;
     int4 m = valid ? p.meta[slot] : make_int4(0, 0, 0, kStatusActive);
     if (valid && m.w == kStatusDone) {
-      const float4 L = p.L[slot];
+      const float4 L = p.bl[2 * slot + 1];
       double* f = p.film_acc + 3LL * m.x;
       atomicAdd(f, static_cast<double>(__fmul_rn(L.x, inv_spp)));
       atomicAdd(f + 1, static_cast<double>(__fmul_rn(L.y, inv_spp)));
@@ -124,11 +124,13 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
         const float upx = smp.next(), upy = smp.next();
         const float ulx = smp.next(), uly = smp.next();
         const Ray ray = camera_ray(v, x, y, upx, upy, ulx, uly);
-        p.ray_o[slot] = make_float4(ray.o.x, ray.o.y, ray.o.z, 0.f);
-        p.ray_d[slot] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f);  // .w: pdf of the last BSDF sample
+        float4* rr = p.ray + 2 * slot;
+        rr[0] = make_float4(ray.o.x, ray.o.y, ray.o.z, 0.f);
+        rr[1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f);  // .w: pdf of the last BSDF sample
         if (p.sort) p.slot_key[slot] = ray_key(p, ray.o, ray.d);
-        p.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-        p.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4* bl = p.bl + 2 * slot;
+        bl[0] = make_float4(1.f, 1.f, 1.f, 0.f);
+        bl[1] = make_float4(0.f, 0.f, 0.f, 0.f);
         const long long film_pix = v.pixel_offset + static_cast<long long>(v.height - y - 1) * v.width + x;
         m = make_int4(static_cast<int>(film_pix), 0, static_cast<int>(smp.state), kStatusActive);
         // PathTracing: while (depth < maxDepth) never runs; Normal and Direct ignore maxDepth
@@ -203,8 +205,9 @@ __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams
         int bin = kBinMiss;
         if (tr.found) {
           const HitRec& h = tr.hit;
-          p.hit_f[slot] = make_float4(h.t, h.u, h.v, 0.f);
-          p.hit_i[slot] = make_int2(h.inst, h.sphere_root ? h.sphere_root : h.tri);
+          float4* hr = p.hit + 2 * slot;
+          hr[0] = make_float4(h.t, h.u, h.v, __int_as_float(h.inst));
+          hr[1] = make_float4(__int_as_float(h.sphere_root ? h.sphere_root : h.tri), 0.f, 0.f, 0.f);
           const DevInstance* I = s.inst + h.inst;
           int m = __ldg(&I->material);
           if (m >= 0 && __ldg(&I->prim_type) == kPrimMesh) {
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams
           }
           bin = m < 0 ? kBinNoMaterial : s.mats[m].type;
         } else {
-          p.hit_i[slot] = make_int2(-1, 0);
+          p.hit[2 * slot] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
         }
         // material binning among the lanes finishing together: equal keys share one atomic
         const unsigned act = __activemask();
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams
       if (!have) {
         if (qi >= n) break;
         slot = p.q_ray[qi];
-        const float4 o = p.ray_o[slot], d = p.ray_d[slot];
+        const float4 o = p.ray[2 * slot], d = p.ray[2 * slot + 1];
         Ray ray;
         ray.o = mk(o.x, o.y, o.z);
         ray.d = mk(d.x, d.y, d.z);
@@ -290,9 +293,9 @@ __device__ __forceinline__ void shade_direct(const WfParams& p, const DevScene& 
   const BsdfSample bs = bsdf_sample(mt, to_local(it.f, wo_w), u_lobe, ubx, uby);
   const V3 nd = to_world(it.f, bs.wi);
   *beta = bs.f;
-  p.ray_o[slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
-  p.ray_d[slot] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
-  p.beta[slot] = make_float4(bs.f.x, bs.f.y, bs.f.z, 0.f);
+  p.ray[2 * slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
+  p.ray[2 * slot + 1] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
+  p.bl[2 * slot] = make_float4(bs.f.x, bs.f.y, bs.f.z, 0.f);
   if (p.sort) p.slot_key[slot] = ray_key(p, it.p, nd);
   *cont = true;
 }
@@ -315,26 +318,27 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
       while (off >= cnt[b]) { off -= cnt[b]; ++b; }
       slot = p.q_bins[static_cast<long long>(b) * p.pool + off];
       int4 m = p.meta[slot];
-      const int2 hi = p.hit_i[slot];
-      if (hi.x < 0) {
+      const float4 hf = p.hit[2 * slot];
+      const int hinst = __float_as_int(hf.w);
+      if (hinst < 0) {
         done = true;
       } else {
-        const float4 o = p.ray_o[slot], d = p.ray_d[slot];
+        const float4 o = p.ray[2 * slot], d = p.ray[2 * slot + 1];
         Ray ray;
         ray.o = mk(o.x, o.y, o.z);
         ray.d = mk(d.x, d.y, d.z);
         const float pdf_bsdf = d.w;
-        const float4 hf = p.hit_f[slot];
+        const int hprim = __float_as_int(p.hit[2 * slot + 1].x);
         HitRec h;
         h.t = hf.x; h.u = hf.y; h.v = hf.z;
-        h.inst = hi.x;
-        const bool sphere = __ldg(&s.inst[hi.x].prim_type) == kPrimSphere;
-        h.tri = sphere ? 0 : hi.y;
-        h.sphere_root = sphere ? hi.y : 0;
+        h.inst = hinst;
+        const bool sphere = __ldg(&s.inst[hinst].prim_type) == kPrimSphere;
+        h.tri = sphere ? 0 : hprim;
+        h.sphere_root = sphere ? hprim : 0;
         const Interaction it = make_interaction(s, ray, h);
-        const float4 b4 = p.beta[slot];
+        const float4 b4 = p.bl[2 * slot];
         V3 beta = mk(b4.x, b4.y, b4.z);
-        float4 L4 = p.L[slot];
+        float4 L4 = p.bl[2 * slot + 1];
         V3 L = mk(L4.x, L4.y, L4.z);
         const int depth = m.y;
         const DevInstance* I = s.inst + it.inst;
@@ -387,10 +391,10 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
             }
             if (alive && depth + 1 < p.max_depth) {
               cont = true;
-              p.ray_o[slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
-              p.ray_d[slot] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
+              p.ray[2 * slot] = make_float4(it.p.x, it.p.y, it.p.z, 0.f);
+              p.ray[2 * slot + 1] = make_float4(nd.x, nd.y, nd.z, bs.pdf);
               if (p.sort) p.slot_key[slot] = ray_key(p, it.p, nd);
-              p.beta[slot] = make_float4(beta.x, beta.y, beta.z, 0.f);
+              p.bl[2 * slot] = make_float4(beta.x, beta.y, beta.z, 0.f);
               m.y = depth + 1;
             } else {
               done = true;
@@ -398,7 +402,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
           }
         }
         }
-        p.L[slot] = make_float4(L.x, L.y, L.z, 0.f);
+        p.bl[2 * slot + 1] = make_float4(L.x, L.y, L.z, 0.f);
         m.z = static_cast<int>(smp.state);
       }
       if (done) m.w = kStatusDone;
@@ -442,11 +446,11 @@ __global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams
           const float4* r = p.shadow + 4LL * rec;
           const int slot = __float_as_int(r[1].w);
           const float4 a = r[2], b = r[3];
-          float4 L = p.L[slot];
+          float4 L = p.bl[2 * slot + 1];
           L.x = fmaf(a.x, b.x, L.x);
           L.y = fmaf(a.y, b.y, L.y);
           L.z = fmaf(a.z, b.z, L.z);
-          p.L[slot] = L;
+          p.bl[2 * slot + 1] = L;
         }
       }
       const int qi = fetch_next(&p.counters[kCntFetchShadow], !have);

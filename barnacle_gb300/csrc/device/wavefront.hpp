@@ -37,13 +37,12 @@ struct WfParams {
   long long total_paths;
   long long n_pixels;
   // per slot
-  float4* ray_o;                // (o, -)
-  float4* ray_d;                // (d, pdf of the last BSDF sample)
-  float4* beta;
-  float4* L;
+  // per slot, 32-byte records so that a slot's part of each is one DRAM sector
+  float4* ray;                  // 2 per slot: (o, -), (d, pdf of the last BSDF sample)
+  float4* bl;                   // 2 per slot: (beta, -), (L, -)
+  float4* hit;                  // 2 per slot: (t, u, v, instance | -1 as int bits),
+                                //             (triangle or sphere root as int bits, -, -, -)
   int4* meta;                   // (film pixel, depth, sampler state, status)
-  float4* hit_f;                // (t, u, v, -)
-  int2* hit_i;                  // (instance | -1, triangle or sphere root)
   // queues
   int* q_active;                // pool entries
   int* q_bins;                  // kNumBins x pool entries
