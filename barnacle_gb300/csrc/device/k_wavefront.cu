@@ -83,35 +83,61 @@ __device__ __forceinline__ void hist_add(unsigned* hist, int key, bool pred) {
   if (pred && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(hist + key, static_cast<unsigned>(__popc(peers)));
 }
 
+// One warp takes kRegenRows rows of 32 slots at a time: their states are loaded together, so a
+// warp has that many independent loads in flight instead of one dependent chain per row, and the
+// path claims and queue appends of all its rows share one atomic each.
+constexpr int kRegenRows = 4;
+
 __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const float inv_spp = __frcp_rn(static_cast<float>(p.spp));
-  const int stride = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+  const int rows = (p.pool + 31) >> 5;
   // the loop runs in whole warps so the warp-wide claims and appends see all 32 lanes
-  const int n = (p.pool + 31) & ~31;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const int slot = base + threadIdx.x;
-    const bool valid = slot < p.pool;
-    int4 m = valid ? p.meta[slot] : make_int4(0, 0, 0, kStatusActive);
-    if (valid && m.w == kStatusDone) {
-      const float4 L = p.bl[2 * slot + 1];
-      double* f = p.film_acc + 3LL * m.x;
-      atomicAdd(f, static_cast<double>(__fmul_rn(L.x, inv_spp)));
-      atomicAdd(f + 1, static_cast<double>(__fmul_rn(L.y, inv_spp)));
-      atomicAdd(f + 2, static_cast<double>(__fmul_rn(L.z, inv_spp)));
-      m.w = kStatusFree;
+  for (int r0 = warp * kRegenRows; r0 < rows; r0 += n_warps * kRegenRows) {
+    int slot[kRegenRows];
+    bool valid[kRegenRows];
+    int4 m[kRegenRows];
+#pragma unroll
+    for (int k = 0; k < kRegenRows; ++k) {
+      slot[k] = (r0 + k) * 32 + lane;
+      valid[k] = slot[k] < p.pool;
+      m[k] = valid[k] ? p.meta[slot[k]] : make_int4(0, 0, 0, kStatusActive);
     }
-    // claim new paths for free slots
-    const bool want = valid && m.w == kStatusFree;
-    const unsigned wmask = __ballot_sync(0xffffffffu, want);
-    if (wmask) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(wmask) - 1;
+    // retire finished paths into the film
+    float4 L[kRegenRows];
+#pragma unroll
+    for (int k = 0; k < kRegenRows; ++k)
+      if (valid[k] && m[k].w == kStatusDone) L[k] = p.bl[2 * slot[k] + 1];
+#pragma unroll
+    for (int k = 0; k < kRegenRows; ++k) {
+      if (valid[k] && m[k].w == kStatusDone) {
+        double* f = p.film_acc + 3LL * m[k].x;
+        atomicAdd(f, static_cast<double>(__fmul_rn(L[k].x, inv_spp)));
+        atomicAdd(f + 1, static_cast<double>(__fmul_rn(L[k].y, inv_spp)));
+        atomicAdd(f + 2, static_cast<double>(__fmul_rn(L[k].z, inv_spp)));
+        m[k].w = kStatusFree;
+      }
+    }
+    // claim new paths for the free slots of all rows with one atomic
+    unsigned wmask[kRegenRows];
+    int nwant = 0;
+#pragma unroll
+    for (int k = 0; k < kRegenRows; ++k) {
+      wmask[k] = __ballot_sync(0xffffffffu, valid[k] && m[k].w == kStatusFree);
+      nwant += __popc(wmask[k]);
+    }
+    if (nwant) {
       unsigned long long first = 0;
-      if (lane == leader) first = atomicAdd(p.work_next, static_cast<unsigned long long>(__popc(wmask)));
-      first = __shfl_sync(0xffffffffu, first, leader);
-      const long long id = static_cast<long long>(first) + __popc(wmask & ((1u << lane) - 1u));
-      if (want && id < p.total_paths) {
+      if (lane == 0) first = atomicAdd(p.work_next, static_cast<unsigned long long>(nwant));
+      first = __shfl_sync(0xffffffffu, first, 0);
+#pragma unroll
+      for (int k = 0; k < kRegenRows; ++k) {
+        const long long id = static_cast<long long>(first) + __popc(wmask[k] & below);
+        first += __popc(wmask[k]);
+        if (!((wmask[k] >> lane) & 1u) || id >= p.total_paths) continue;
         const int vi = find_view(p, id);
         const DevView& v = p.views[vi];
         const long long local = id - v.path_offset;
@@ -124,28 +150,43 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
         const float upx = smp.next(), upy = smp.next();
         const float ulx = smp.next(), uly = smp.next();
         const Ray ray = camera_ray(v, x, y, upx, upy, ulx, uly);
-        float4* rr = p.ray + 2 * slot;
+        float4* rr = p.ray + 2 * slot[k];
         rr[0] = make_float4(ray.o.x, ray.o.y, ray.o.z, 0.f);
         rr[1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f);  // .w: pdf of the last BSDF sample
-        if (p.sort) p.slot_key[slot] = ray_key(p, ray.o, ray.d);
-        float4* bl = p.bl + 2 * slot;
+        if (p.sort) p.slot_key[slot[k]] = ray_key(p, ray.o, ray.d);
+        float4* bl = p.bl + 2 * slot[k];
         bl[0] = make_float4(1.f, 1.f, 1.f, 0.f);
         bl[1] = make_float4(0.f, 0.f, 0.f, 0.f);
         const long long film_pix = v.pixel_offset + static_cast<long long>(v.height - y - 1) * v.width + x;
-        m = make_int4(static_cast<int>(film_pix), 0, static_cast<int>(smp.state), kStatusActive);
+        m[k] = make_int4(static_cast<int>(film_pix), 0, static_cast<int>(smp.state), kStatusActive);
         // PathTracing: while (depth < maxDepth) never runs; Normal and Direct ignore maxDepth
-        if (p.max_depth <= 0 && p.integrator == BN_INTEGRATOR_PATH) m.w = kStatusDone;
+        if (p.max_depth <= 0 && p.integrator == BN_INTEGRATOR_PATH) m[k].w = kStatusDone;
       }
     }
-    const bool active = valid && m.w == kStatusActive;
-    const int qi = warp_append(&p.counters[kCntActive], active);
-    if (active) p.q_active[qi] = slot;
-    if (p.sort) {
-      const int key = active ? p.slot_key[slot] : 0;
-      if (active) p.q_key[qi] = key;
-      hist_add(p.hist, key, active);
+    // append the active slots of all rows to the ray queue with one atomic
+    unsigned amask[kRegenRows];
+    int nact = 0;
+#pragma unroll
+    for (int k = 0; k < kRegenRows; ++k) {
+      amask[k] = __ballot_sync(0xffffffffu, valid[k] && m[k].w == kStatusActive);
+      nact += __popc(amask[k]);
     }
-    if (valid) p.meta[slot] = m;
+    int qbase = 0;
+    if (nact && lane == 0) qbase = atomicAdd(&p.counters[kCntActive], nact);
+    qbase = __shfl_sync(0xffffffffu, qbase, 0);
+#pragma unroll
+    for (int k = 0; k < kRegenRows; ++k) {
+      const bool active = (amask[k] >> lane) & 1u;
+      const int qi = qbase + __popc(amask[k] & below);
+      qbase += __popc(amask[k]);
+      if (active) p.q_active[qi] = slot[k];
+      if (p.sort) {
+        const int key = active ? p.slot_key[slot[k]] : 0;
+        if (active) p.q_key[qi] = key;
+        hist_add(p.hist, key, active);
+      }
+      if (valid[k]) p.meta[slot[k]] = m[k];
+    }
   }
 }
 
