@@ -17,11 +17,12 @@
 //    walked wide (kWalkWide) when the upload built records for it (large scenes; small BVHs gain
 //    nothing from them).  The counting walk (kWalkCount) is always the binary one, so its counts
 //    equal the reference's (the root plus both children of every entered interior node).
-//  * the walk is a flat state machine: each step is one bounded unit of work (a node record,
-//    one triangle or one instance) at either BVH level, with pops folded into the step that
-//    needs them, so lanes at different levels run the same loop body and reconverge after every
-//    step instead of waiting out each other's nested BLAS loops.  A caller can refill a lane
-//    with a new ray as soon as its walk finishes.
+//  * the walk is a flat state machine: each step is one bounded unit of work (a node record or
+//    pair, a leaf's triangles, a TLAS leaf's instances) at either BVH level, with pops folded
+//    into the step that needs them, so lanes at different levels run the same loop body and
+//    reconverge after every step instead of waiting out each other's nested BLAS loops.  A
+//    caller can refill a lane with a new ray as soon as its walk finishes, and let only the
+//    lanes at one kind of unit take a step (trav_vote).
 
 namespace bn {
 

@@ -1,11 +1,15 @@
 // The batched wavefront form of PathTracingIntegrator.Li (PathTracing.fs:14-81) over many views.
 //
-// A pool of P path slots lives in HBM (SoA).  One iteration of the bounce loop is:
-//   regen    every slot: retire a finished path into the FP64 film, refill free slots with new
-//            camera paths (warp-aggregated claims on a global path counter), and append the
-//            active slots to the ray queue (ballot + popc compaction) with their sort keys
+// A pool of P path slots lives in HBM, one array per kind of record (WfParams: each slot's ray,
+// throughput + radiance and hit are 32-byte records, one DRAM sector each).  One iteration of the
+// bounce loop is:
+//   regen    every slot (four 32-slot rows per warp): retire a finished path into the FP64 film,
+//            refill free slots with new camera paths (warp-aggregated claims on a global path
+//            counter), and append the active slots to the ray queue (ballot + popc compaction)
+//            with their sort keys
 //   sort     counting sort of the ray queue by key (octant, origin cell): scan + scatter
-//   extend   closest hit for the ray queue; each hit is binned by the material type it shades
+//   extend   closest hit for the ray queue (persistent lanes that vote on the kind of traversal
+//            step, trav_vote); each hit is binned by the material type it shades
 //            with (__match_any_sync groups, one atomic per group) so shading runs type-sorted
 //   shade    emission with MIS, light sample + BSDF eval (a shadow-ray record), BSDF sample,
 //            Russian roulette; marks paths that end
@@ -27,9 +31,9 @@ namespace {
 
 constexpr int kStatusFree = 0, kStatusActive = 1, kStatusDone = 2;
 constexpr int kBinMiss = 4, kBinNoMaterial = 5;
-// the wavefront's traversal step: one wide record, a whole BLAS leaf (at most 4 triangles), or a
-// TLAS leaf's instances until one is entered; only the lanes that win the mode vote (trav_vote)
-// take it
+// the wavefront's traversal step: one wide record, up to 4 triangles of a BLAS leaf (a whole leaf
+// but for the builder's depth-capped ones), or a TLAS leaf's instances until one is entered; only
+// the lanes that win the mode vote (trav_vote) take it
 constexpr int kWfTris = 4;
 constexpr bool kWfInstRun = true;
 // blocks of 128 per SM the traversal kernels are compiled for (registers: 65,536 / (128 x blocks))
