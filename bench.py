@@ -262,6 +262,27 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def profile_figures(mode, workload, spp_per_step):
+    """The ncu figures committed under profiles/ for this form and workload: the DRAM bytes of one
+    render ("bytes_per_launch: N", measured at 4 spp per step; other step sizes report none) and
+    the L2 side of the roofline of the dominant kernel ("l2: kernel=… hit_rate=… throughput_frac=…")."""
+    traffic = None
+    prof = ROOT / "profiles" / f"traffic_{mode}_{workload}.md"
+    if prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("bytes_per_launch:") and spp_per_step == 4:
+                traffic = int(line.split(":")[1])
+    l2 = None
+    prof = ROOT / "profiles" / ("k_pt_mega_instances.md" if mode == "megakernel" else "k_wf_extend_instances.md")
+    if workload == "instances" and prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("l2:"):
+                kv = dict(f.split("=") for f in line[3:].split())
+                l2 = {"kernel": kv["kernel"], "hit_rate": float(kv["hit_rate"]),
+                      "throughput_frac": float(kv["throughput_frac"]), "source": f"profiles/{prof.name} (ncu)"}
+    return traffic, l2
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -374,21 +395,7 @@ def main():
     peak, peak_kind = measured_peak_gbs()
     dom_launch_s = dom_ms / 1000.0 / args.steps
     achieved = alg_bytes / dom_launch_s / 1e9
-    traffic = None
-    prof = ROOT / "profiles" / f"traffic_{args.mode}_{args.workload}.md"
-    if prof.exists():  # an ncu summary with a "bytes_per_launch: N" line
-        for line in prof.read_text().splitlines():
-            if line.startswith("bytes_per_launch:"):
-                # measured at the default 4 spp per step; other step sizes report none
-                traffic = int(line.split(":")[1]) if args.spp_per_step == 4 else None
-    l2 = None  # the L2 side of the roofline, from the ncu summary of the dominant kernel
-    prof = ROOT / "profiles" / ("k_pt_mega_instances.md" if args.mode == "megakernel" else "k_wf_extend_instances.md")
-    if args.workload == "instances" and prof.exists():
-        for line in prof.read_text().splitlines():
-            if line.startswith("l2:"):
-                kv = dict(f.split("=") for f in line[3:].split())
-                l2 = {"kernel": kv["kernel"], "hit_rate": float(kv["hit_rate"]),
-                      "throughput_frac": float(kv["throughput_frac"]), "source": f"profiles/{prof.name} (ncu)"}
+    traffic, l2 = profile_figures(args.mode, args.workload, args.spp_per_step)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

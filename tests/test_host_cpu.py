@@ -409,3 +409,22 @@ def test_json_loader_interpolates_keyframes_around_time_zero(tmp_path):
     p.write_text(json.dumps(scene([{"time": 0, "translation": [5, 0, 0]}, {"time": 2, "translation": [9, 0, 0]}])))
     m = np.array(Bundle.load_json(str(p)).scene.contents.instances[0].object_to_world, np.float32).reshape(4, 4)
     assert list(m[3, :3]) == [5, 0, 0]
+
+
+def test_bench_reads_the_committed_profile_figures():
+    """bench.py reports the DRAM traffic and the L2 side of the roofline from the ncu summaries
+    under profiles/; their machine-readable lines must parse and hold plausible values."""
+    sys_path = str(ROOT)
+    import sys
+    if sys_path not in sys.path:
+        sys.path.insert(0, sys_path)
+    import bench
+
+    traffic, l2 = bench.profile_figures("wavefront", "instances", 4)
+    assert traffic is not None and 10 ** 9 < traffic < 10 ** 13
+    assert l2["kernel"] == "k_wf_extend" and 0 < l2["hit_rate"] < 1 and 0 < l2["throughput_frac"] < 1
+    traffic, l2 = bench.profile_figures("wavefront", "instances", 8)
+    assert traffic is None  # measured at 4 spp per step only
+    _, l2 = bench.profile_figures("megakernel", "instances", 4)
+    assert l2["kernel"] == "k_pt_mega" and 0 < l2["hit_rate"] < 1
+    assert bench.profile_figures("megakernel", "cornell", 4) == (None, None)
