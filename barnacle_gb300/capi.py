@@ -33,6 +33,7 @@ BN_INTEGRATOR_PATH, BN_INTEGRATOR_PSSMLT, BN_INTEGRATOR_NORMAL, BN_INTEGRATOR_DI
 BN_MODE_MEGAKERNEL, BN_MODE_WAVEFRONT = 0, 1
 BN_MUTATION_GAUSSIAN, BN_MUTATION_KELEMEN = 0, 1
 BN_RENDER_WATERTIGHT, BN_RENDER_FIXED_ALIAS, BN_RENDER_NO_GRAPH, BN_RENDER_COUNT = 0x1, 0x2, 0x4, 0x8
+BN_RENDER_CULL_SHADOW = 0x10
 BN_DEVERR_STACK_OVERFLOW, BN_DEVERR_QUEUE_OVERFLOW, BN_DEVERR_WATCHDOG, BN_DEVERR_BAD_INDEX = 0x1, 0x2, 0x4, 0x8
 
 
@@ -166,6 +167,7 @@ SIGNATURES = {
     "bn_film_tonemap": (C.c_int, [P, C.c_int32, P, C.c_int64]),
     "bn_image_write_png": (C.c_int, [C.c_char_p, P, C.c_int32, C.c_int32]),
     "bn_render_noalloc": (C.c_int, [P, C.POINTER(bn_render_desc), C.POINTER(bn_view), C.c_int32, P]),
+    "bn_set_limits": (C.c_int, [P, C.c_int32, C.c_int32]),
     "bn_get_stats": (C.c_int, [P, C.POINTER(bn_stats)]),
     "bn_reset_stats": (C.c_int, [P]),
     "bn_forward": (C.c_int, [P, C.POINTER(bn_adjoint_desc), P, P, P]),

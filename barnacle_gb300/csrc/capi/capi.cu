@@ -37,6 +37,40 @@ bn::DevView make_dev_view(const bn_view& v, long long pixel_offset, long long pa
   return d;
 }
 
+MegaChunks mega_chunks(long long pixels, int spp, long long max_items) {
+  // work items: pixels x chunks per view; enough threads to fill 152 SMs several times
+  const long long target = 152LL * 2048 * 4;
+  long long chunks = std::min<long long>(spp, std::max<long long>(1, (target + pixels - 1) / pixels));
+  // a caller with a fixed scratch size: fewer, longer chunks until the partial sums fit
+  if (max_items > 0) chunks = std::max<long long>(1, std::min<long long>(chunks, max_items / std::max(1LL, pixels)));
+  const long long spc = (spp + chunks - 1) / chunks;
+  MegaChunks c;
+  c.spc = static_cast<int>(spc);
+  c.chunks = static_cast<int>((spp + spc - 1) / spc);
+  return c;
+}
+
+bn::MegaParams mega_params(const bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views,
+                           const MegaChunks& ck, long long items, long long pixels) {
+  bn::MegaParams p{};
+  p.n_views = static_cast<int>(views.size());
+  p.n_items = items;
+  p.spp = d->spp;
+  p.chunks = ck.chunks;
+  p.spc = ck.spc;
+  p.max_depth = d->max_depth;
+  p.rr_depth = d->rr_depth;
+  p.frame_id = d->frame_id;
+  p.integrator = d->integrator;
+  p.simple = ctx->scene_simple;
+  for (const bn::DevView& v : views)
+    if (v.cam_type == BN_CAM_THIN_LENS && v.aperture > 0.f) p.simple = false;
+  p.watertight = d->flags & BN_RENDER_WATERTIGHT;
+  p.n_pixels = pixels;
+  p.counters = ctx->counters.as<bn::DevCounters>();
+  return p;
+}
+
 int check_device_error(bn_context* ctx) {
   unsigned int w = 0;
   cudaError_t e = cudaMemcpyAsync(&w, ctx->error_word.ptr, sizeof(w), cudaMemcpyDeviceToHost, ctx->stream);
@@ -63,18 +97,14 @@ int read_counters(bn_context* ctx, bn::DevCounters* out) {
 }
 
 int render_megakernel(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views, bool count) {
-  // work items: pixels x chunks per view; enough threads to fill 152 SMs several times
   long long pixels = 0;
   for (const auto& v : views) pixels += static_cast<long long>(v.width) * v.height;
-  const long long target = 152LL * 2048 * 4;
-  int chunks = static_cast<int>(std::min<long long>(d->spp, std::max<long long>(1, (target + pixels - 1) / pixels)));
-  const int spc = (d->spp + chunks - 1) / chunks;
-  chunks = (d->spp + spc - 1) / spc;
+  const bnc::MegaChunks ck = bnc::mega_chunks(pixels, d->spp, 0);
   std::vector<long long> item_off(views.size());
   long long items = 0;
   for (size_t i = 0; i < views.size(); ++i) {
     item_off[i] = items;
-    items += static_cast<long long>(views[i].width) * views[i].height * chunks;
+    items += static_cast<long long>(views[i].width) * views[i].height * ck.chunks;
   }
   cudaError_t e;
   if ((e = ctx->item_offsets.reserve(item_off.size() * sizeof(long long))) != cudaSuccess)
@@ -83,27 +113,13 @@ int render_megakernel(bn_context* ctx, const bn_render_desc* d, const std::vecto
     return ctx->cuda_fail(e, "alloc partial sums");
   cudaMemcpyAsync(ctx->item_offsets.ptr, item_off.data(), item_off.size() * sizeof(long long), cudaMemcpyHostToDevice,
                   ctx->stream);
-  bn::MegaParams p{};
+  bn::MegaParams p = bnc::mega_params(ctx, d, views, ck, items, pixels);
   p.views = ctx->views.as<bn::DevView>();
-  p.n_views = static_cast<int>(views.size());
-  p.n_items = items;
   p.item_offsets = ctx->item_offsets.as<long long>();
-  p.spp = d->spp;
-  p.chunks = chunks;
-  p.spc = spc;
-  p.max_depth = d->max_depth;
-  p.rr_depth = d->rr_depth;
-  p.frame_id = d->frame_id;
-  p.integrator = d->integrator;
-  p.simple = ctx->scene_simple;
-  for (const bn::DevView& v : views)
-    if (v.cam_type == BN_CAM_THIN_LENS && v.aperture > 0.f) p.simple = false;
-  p.watertight = d->flags & BN_RENDER_WATERTIGHT;
   p.count = count;
+  p.cull = d->flags & BN_RENDER_CULL_SHADOW;
   p.partial = ctx->partial.as<float4>();
   p.film = ctx->film.as<float>();
-  p.n_pixels = pixels;
-  p.counters = ctx->counters.as<bn::DevCounters>();
   cudaEventRecord(ctx->ev0, ctx->stream);
   if ((e = bn::launch_megakernel(ctx->scene, p, ctx->stream)) != cudaSuccess) return ctx->cuda_fail(e, "megakernel launch");
   cudaEventRecord(ctx->ev1, ctx->stream);
@@ -341,6 +357,17 @@ int bn_film_tonemap(bn_context* ctx, int32_t tone_mapping, uint8_t* rgba, int64_
   e = cudaMemcpyAsync(rgba, ctx->rgba.ptr, static_cast<size_t>(n_pixels) * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return e == cudaSuccess ? BN_OK : ctx->cuda_fail(e, "tone-mapped film download");
+}
+
+int bn_set_limits(bn_context* ctx, int32_t stack_entries, int32_t max_bounce_iterations) {
+  if (!ctx) return BN_ERR_INVALID_ARG;
+  if (stack_entries < 0 || stack_entries > bn::kStackSize || max_bounce_iterations < 0)
+    return ctx->fail(BN_ERR_INVALID_ARG, "bn_set_limits: stack entries 0.." + std::to_string(bn::kStackSize) +
+                                             ", iterations >= 0 (0 = default)");
+  ctx->limit_stack = stack_entries;
+  ctx->limit_iters = max_bounce_iterations;
+  ctx->scene.stack_cap = stack_entries > 0 ? stack_entries : bn::kStackSize;
+  return BN_OK;
 }
 
 int bn_get_stats(const bn_context* ctx, bn_stats* out) {

@@ -8,6 +8,7 @@
 #include "../../../include/barnacle_gpu.h"
 #include "../device/dev_types.cuh"
 #include "../device/launch.hpp"
+#include "../device/pssmlt.hpp"
 
 // growable device buffer
 struct DevBuf {
@@ -47,6 +48,9 @@ struct bn_context {
   int n_lights = 0;
   float scene_lo[3] = {0.f, 0.f, 0.f}, scene_hi[3] = {0.f, 0.f, 0.f};  // TLAS root box
   bool scene_simple = false;  // Lambertian materials, triangle meshes, the uniform light sampler
+  // failure-detection limits (bn_set_limits; 0 = the defaults)
+  int limit_stack = 0;        // traversal stack entries a walk may use
+  int limit_iters = 0;        // wavefront bounce-loop iterations before the watchdog stops it
 
   // queries
   DevBuf q_in, q_out;
@@ -78,9 +82,21 @@ namespace bnc {
 // host-side view constants (Extensions/Camera/Pinhole.fs:16-22), shared by all render modes
 bn::DevView make_dev_view(const bn_view& v, long long pixel_offset, long long path_offset);
 int check_device_error(bn_context* ctx);
+// The plain megakernel's sample chunks: each work item runs spc consecutive samples of one pixel,
+// chunks = ceil(spp / spc) items per pixel.  max_items > 0 caps pixels * chunks (fixed scratch).
+struct MegaChunks {
+  int chunks = 1, spc = 1;
+};
+MegaChunks mega_chunks(long long pixels, int spp, long long max_items);
+// Launch parameters of the megakernel shared by bn_render and bn_render_noalloc (views, item
+// offsets, partial sums, film and counting are filled in by the caller).
+bn::MegaParams mega_params(const bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views,
+                           const MegaChunks& ck, long long items, long long pixels);
 int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views);
 // BVHNode.Build on the GPU (bvh_gpu.cu): the host builder's nodes and permutation
 int gpu_bvh_build(bn_context* ctx, const float* bounds, int32_t n, std::vector<bn_bvh_node>* nodes,
                   std::vector<int32_t>* perm, int small);
 int render_pssmlt(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views);
+// the PSSMLT chains in the wavefront (wavefront.cu), after the bootstrap
+int render_pssmlt_wavefront(bn_context* ctx, const bn_render_desc* d, const bn::MltParams& mp, int* launches);
 }  // namespace bnc

@@ -49,6 +49,8 @@ int render_pssmlt(bn_context* ctx, const bn_render_desc* d, const std::vector<bn
   const bn::DevView& v = views[0];
   const long long pixels = static_cast<long long>(v.width) * v.height;
   const int dims = 4 + 7 * d->max_depth;
+  if (d->mode == BN_MODE_WAVEFRONT && dims >= 4096)
+    return ctx->fail(BN_ERR_UNSUPPORTED, "wavefront PSSMLT supports max_depth up to 584");
   const long long mpc_ll = (static_cast<long long>(d->spp) * pixels + d->n_chains - 1) / d->n_chains;
   if (mpc_ll > (1LL << 30)) return ctx->fail(BN_ERR_INVALID_ARG, "too many mutations per chain");
   cudaError_t e;
@@ -76,7 +78,7 @@ int render_pssmlt(bn_context* ctx, const bn_render_desc* d, const std::vector<bn
   p.eps_max = d->eps_max;
   p.watertight = d->flags & BN_RENDER_WATERTIGHT;
   p.weights = ctx->mlt_boot.as<float>();
-  p.X = ctx->mlt_state.as<float4>();
+  p.X = ctx->mlt_state.as<float4>();  // [dimension][chain] (lockstep) or [chain][dimension] (wavefront)
   p.film = ctx->film.as<float>();
   p.accepted = reinterpret_cast<unsigned long long*>(ctx->mlt_chain.ptr);
   cudaMemsetAsync(ctx->film.ptr, 0, static_cast<size_t>(pixels) * 3 * sizeof(float), st);
@@ -110,8 +112,16 @@ int render_pssmlt(bn_context* ctx, const bn_render_desc* d, const std::vector<bn
       p.alias_idx = didx;
     }
     cudaEventRecord(ctx->ev1, st);
-    if ((e = bn::launch_mlt_chains(p, st)) != cudaSuccess) return ctx->cuda_fail(e, "chain launch");
-    ++launches;
+    if (d->mode == BN_MODE_WAVEFRONT) {
+      // the chains compacted every bounce (wavefront.cu, k_mlt_wavefront.cu)
+      int wl = 0;
+      const int rc = bnc::render_pssmlt_wavefront(ctx, d, p, &wl);
+      if (rc) return rc;
+      launches += wl;
+    } else {
+      if ((e = bn::launch_mlt_chains(p, st)) != cudaSuccess) return ctx->cuda_fail(e, "chain launch");
+      ++launches;
+    }
   } else {
     cudaEventRecord(ctx->ev1, st);
   }

@@ -14,8 +14,12 @@
 //
 //  * limits: at most kMaxViews (64) views and kMaxItems (1,048,576) partial sums, i.e. 16 MiB of
 //    partial sums; every GPU that loads the library holds the array until the process exits.
-//    A render with more than kMaxItems pixels in total is rejected; otherwise the sample chunks
-//    are lengthened until the partial sums fit.
+//    A render with more than kMaxItems pixels in total is rejected.  While pixels x bn_render's
+//    chunks per pixel fit the array the image is bit-identical to bn_render's; beyond that the
+//    call uses fewer, longer sample chunks, so each chunk sums more samples and the image equals
+//    bn_render's only up to float summation order (the per-path radiance is the same).
+//  * not supported: BN_RENDER_COUNT (visit counting needs no scratch-free form); the context's own
+//    film (bn_film_download, bn_film_tonemap) is not written, it keeps the last bn_render's image.
 //  * set-up: the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (with that device current; this may load the library's device code on
 //    that GPU).  Make the first call on each device before any stream capture.
@@ -72,10 +76,23 @@ extern "C" int bn_render_noalloc(bn_context* ctx, const bn_render_desc* d, const
                                              std::to_string(n_views));
   if (d->integrator != BN_INTEGRATOR_PATH || d->mode != BN_MODE_MEGAKERNEL)
     return ctx->fail(BN_ERR_UNSUPPORTED, "bn_render_noalloc renders the path-tracing megakernel mode only");
+  if (d->flags & BN_RENDER_COUNT)
+    return ctx->fail(BN_ERR_UNSUPPORTED, "bn_render_noalloc does not count visits (BN_RENDER_COUNT): use bn_render");
   if (d->spp <= 0 || d->max_depth < 0 || d->rr_depth < 0)
     return ctx->fail(BN_ERR_INVALID_ARG, "bn_render_noalloc: spp must be positive, depths non-negative");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "bn_render_noalloc: cudaSetDevice");
+  // the film must be device memory of this context's GPU: a host pointer or another GPU's memory
+  // would make the reduction kernel fault
+  cudaPointerAttributes attr{};
+  e = cudaPointerGetAttributes(&attr, film_device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return ctx->fail(BN_ERR_INVALID_ARG, "bn_render_noalloc: film_device is not a CUDA pointer");
+  }
+  if ((attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) || attr.device != ctx->device)
+    return ctx->fail(BN_ERR_INVALID_ARG, "bn_render_noalloc: film_device must be device memory of GPU " +
+                                             std::to_string(ctx->device));
   NoAllocScratch* scratch = nullptr;
   int rc = scratch_for_device(ctx, &scratch);
   if (rc) return rc;
@@ -90,20 +107,13 @@ extern "C" int bn_render_noalloc(bn_context* ctx, const bn_render_desc* d, const
   if (pixels > kMaxItems)
     return ctx->fail(BN_ERR_INVALID_ARG, "bn_render_noalloc: " + std::to_string(pixels) + " pixels exceed the " +
                                              std::to_string(kMaxItems) + "-pixel limit of its static scratch");
-  // the chunking of bn_render's megakernel mode, then longer chunks until the partials fit
-  const long long target = 152LL * 2048 * 4;
-  int chunks = static_cast<int>(std::min<long long>(d->spp, std::max<long long>(1, (target + pixels - 1) / pixels)));
-  int spc = (d->spp + chunks - 1) / chunks;
-  chunks = (d->spp + spc - 1) / spc;
-  while (pixels * chunks > kMaxItems) {
-    ++spc;
-    chunks = (d->spp + spc - 1) / spc;
-  }
+  // bn_render's chunking, capped so that the partial sums fit the array
+  const bnc::MegaChunks ck = bnc::mega_chunks(pixels, d->spp, kMaxItems);
   std::vector<long long> item_off(n_views);
   long long items = 0;
   for (int i = 0; i < n_views; ++i) {
     item_off[i] = items;
-    items += static_cast<long long>(views[i].width) * views[i].height * chunks;
+    items += static_cast<long long>(views[i].width) * views[i].height * ck.chunks;
   }
   if ((e = cudaMemcpyAsync(scratch->views, dv.data(), dv.size() * sizeof(bn::DevView), cudaMemcpyHostToDevice,
                            ctx->stream)) != cudaSuccess ||
@@ -111,23 +121,13 @@ extern "C" int bn_render_noalloc(bn_context* ctx, const bn_render_desc* d, const
                            cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
     return ctx->cuda_fail(e, "bn_render_noalloc: view upload");
 
-  bn::MegaParams p{};
+  bn::MegaParams p = bnc::mega_params(ctx, d, dv, ck, items, pixels);
   p.views = scratch->views;
-  p.n_views = n_views;
-  p.n_items = items;
   p.item_offsets = scratch->item_offsets;
-  p.spp = d->spp;
-  p.chunks = chunks;
-  p.spc = spc;
-  p.max_depth = d->max_depth;
-  p.rr_depth = d->rr_depth;
-  p.frame_id = d->frame_id;
-  p.watertight = d->flags & BN_RENDER_WATERTIGHT;
   p.count = false;
+  p.cull = d->flags & BN_RENDER_CULL_SHADOW;
   p.partial = scratch->partial;
   p.film = film_device;
-  p.n_pixels = pixels;
-  p.counters = ctx->counters.as<bn::DevCounters>();
   cudaEventRecord(ctx->ev0, ctx->stream);
   if ((e = bn::launch_megakernel(ctx->scene, p, ctx->stream)) != cudaSuccess)
     return ctx->cuda_fail(e, "bn_render_noalloc: megakernel launch");

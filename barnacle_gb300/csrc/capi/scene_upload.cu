@@ -463,6 +463,7 @@ extern "C" int bn_scene_upload(bn_context* ctx, const bn_scene_desc* d) {
   s.n_tri_lights = static_cast<int>(tl.size());
   s.light_sampler = d->light_sampler;
   s.n_mats = d->n_materials;
+  s.stack_cap = ctx->limit_stack > 0 ? ctx->limit_stack : bn::kStackSize;
   s.error_word = ctx->error_word.as<unsigned int>();
   for (int a = 0; a < 3; ++a) {
     ctx->scene_lo[a] = tlas[0].bounds_min[a];

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "../device/pssmlt.hpp"
 #include "../device/wavefront.hpp"
 #include "context.hpp"
 
@@ -14,6 +15,7 @@ namespace {
 struct WfState {
   int pool = 0;
   DevBuf params, ray, bl, hit, meta, q_active, q_bins, shadow, counters, work_next, film_acc;
+  DevBuf mlt_smp, mlt_chain;  // PSSMLT chains: sampler state and chain records
   DevBuf slot_key, q_key, q_ray, sh_key, q_shadow, hist, off;
   // captured graph (one per launch shape)
   cudaGraph_t graph = nullptr;
@@ -22,14 +24,14 @@ struct WfState {
   bool graph_failed = false;
   bn::WfLaunch shape{};
   int shape_cap = -1;
-  // autotuned choice per uploaded scene
-  long long tuned_generation = -1;
-  bool tuned_watertight = false;
-  int tuned_pool = 0, tuned_cap = 0;
+  // autotuned choice per uploaded scene and triangle test (index: watertight)
+  long long tuned_generation[2] = {-1, -1};
+  int tuned_pool[2] = {0, 0}, tuned_cap[2] = {0, 0};
 
   void release() {
     DevBuf* b[] = {&params, &ray, &bl, &hit, &meta, &q_active, &q_bins, &shadow, &counters,
-                   &work_next, &film_acc, &slot_key, &q_key, &q_ray, &sh_key, &q_shadow, &hist, &off};
+                   &work_next, &film_acc, &slot_key, &q_key, &q_ray, &sh_key, &q_shadow, &hist, &off,
+                   &mlt_smp, &mlt_chain};
     for (DevBuf* x : b) x->release();
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -121,7 +123,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   const bool sort = true, sort_shadow = true;
   const bool count = d->flags & BN_RENDER_COUNT;
   if (w->shape_cap != cap || w->shape.watertight != wt || w->shape.wide != wide || w->shape.sort != sort ||
-      w->shape.sort_shadow != sort_shadow || w->shape.count != count) {
+      w->shape.sort_shadow != sort_shadow || w->shape.count != count || w->shape.mlt) {
     w->shape = bn::wf_launch_shape(wt, wide, sort, sort_shadow, count, cap);
     w->shape_cap = cap;
     if (w->exec) {
@@ -146,6 +148,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.total_paths = total_paths;
   p.n_pixels = n_pixels;
   p.max_iters = static_cast<int>(std::min<long long>(1LL << 30, (total_paths / pool + 2) * (d->max_depth + 2) + 64));
+  if (ctx->limit_iters > 0) p.max_iters = ctx->limit_iters;
   p.ray = w->ray.as<float4>();
   p.bl = w->bl.as<float4>();
   p.hit = w->hit.as<float4>();
@@ -225,9 +228,122 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   return BN_OK;
 }
 
+// The bounce loop of PSSMLT chains (one slot per chain), enqueued on the context's stream after
+// the bootstrap: a graph launch, or host-driven iterations with BN_RENDER_NO_GRAPH.  Splats go
+// straight into ctx->film.  Returns the iterations run through *iters.
+int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltParams& mp, int* iters) {
+  cudaError_t e;
+  const int pool = mp.n_chains;
+  if ((e = ensure_pool(w, pool)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront chain-state allocation");
+  if ((e = w->mlt_smp.reserve(static_cast<size_t>(pool) * sizeof(int4))) != cudaSuccess ||
+      (e = w->mlt_chain.reserve(static_cast<size_t>(pool) * 3 * sizeof(float4))) != cudaSuccess)
+    return ctx->cuda_fail(e, "wavefront chain records");
+  const bool wt = d->flags & BN_RENDER_WATERTIGHT;
+  const bool wide = ctx->scene.wide != 0;
+  if (!w->shape.mlt || w->shape.watertight != wt || w->shape.wide != wide) {
+    // 65,536 chains are few rays per launch: the queues are traversed unsorted
+    w->shape = bn::wf_launch_shape(wt, wide, false, false, false, 0, true);
+    w->shape_cap = -1;
+    if (w->exec) {
+      cudaGraphExecDestroy(w->exec);
+      w->exec = nullptr;
+    }
+  }
+  bool use_graph = !(d->flags & BN_RENDER_NO_GRAPH);
+  bn::WfParams p{};
+  p.scene = ctx->scene;
+  p.views = mp.view;
+  p.n_views = 1;
+  p.spp = d->spp;
+  p.max_depth = d->max_depth;
+  p.rr_depth = d->rr_depth;
+  p.frame_id = d->frame_id;
+  p.integrator = BN_INTEGRATOR_PSSMLT;
+  p.pool = pool;
+  p.refill_extend = 16;
+  p.refill_shadow = 16;
+  p.total_paths = 0;
+  p.n_pixels = 0;
+  // a mutation's path takes at most max_depth iterations (at least one)
+  p.max_iters = static_cast<int>(std::min<long long>(
+      1LL << 30, (static_cast<long long>(mp.mutations_per_chain) + 1) * std::max(1, d->max_depth) + 64));
+  if (ctx->limit_iters > 0) p.max_iters = ctx->limit_iters;
+  p.ray = w->ray.as<float4>();
+  p.bl = w->bl.as<float4>();
+  p.hit = w->hit.as<float4>();
+  p.meta = w->meta.as<int4>();
+  p.q_active = w->q_active.as<int>();
+  p.sort = 0;
+  p.sort_shadow = 0;
+  p.q_ray = w->q_active.as<int>();
+  p.q_bins = w->q_bins.as<int>();
+  p.shadow = w->shadow.as<float4>();
+  p.counters = w->counters.as<int>();
+  p.trace_counters = ctx->counters.ptr;
+  p.work_next = w->work_next.as<unsigned long long>();
+  p.film_out = mp.film;
+  p.mlt = 1;
+  bn::MltWf& q = p.mlt_p;
+  q.n_chains = mp.n_chains;
+  q.n_bootstrap = mp.n_bootstrap;
+  q.n_dims = mp.n_dims;
+  q.mutations = mp.mutations_per_chain;
+  q.kelemen = mp.kelemen;
+  q.p_large = mp.large_step_prob;
+  q.sigma = mp.sigma;
+  q.eps_min = mp.eps_min;
+  q.eps_max = mp.eps_max;
+  q.b = mp.b;
+  q.inv_eff_spp = mp.inv_eff_spp;
+  q.alias_prob = mp.alias_prob;
+  q.alias_idx = mp.alias_idx;
+  q.smp = w->mlt_smp.as<int4>();
+  q.chain = w->mlt_chain.as<float4>();
+  q.X = mp.X;
+  q.film = mp.film;
+  q.accepted = mp.accepted;
+  if (use_graph && !w->exec && !w->graph_failed) {
+    if (build_graph(ctx, w) != BN_OK) {
+      w->graph_failed = true;
+      use_graph = false;
+    }
+  }
+  if (use_graph && !w->exec) use_graph = false;
+  p.cond = w->cond;
+  cudaStream_t st = ctx->stream;
+  cudaMemcpyAsync(w->params.ptr, &p, sizeof(p), cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(w->counters.ptr, 0, bn::kCntSize * sizeof(int), st);
+  cudaMemsetAsync(w->meta.ptr, 0, static_cast<size_t>(pool) * sizeof(int4), st);  // every chain unstarted
+  if (use_graph) {
+    if ((e = cudaGraphLaunch(w->exec, st)) != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphLaunch");
+  } else {
+    for (int it = 0; it < p.max_iters + 1; ++it) {
+      if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st)) != cudaSuccess)
+        return ctx->cuda_fail(e, "wavefront chain iteration launch");
+      int again = 0;
+      cudaMemcpyAsync(&again, w->counters.as<int>() + bn::kCntAgain, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront chain iteration");
+      if (!again) break;
+    }
+  }
+  int counters[bn::kCntSize];
+  e = cudaMemcpyAsync(counters, w->counters.ptr, sizeof(counters), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "wavefront chains");
+  *iters = counters[bn::kCntIter];
+  return BN_OK;
+}
+
 }  // namespace
 
 namespace bnc {
+
+int render_pssmlt_wavefront(bn_context* ctx, const bn_render_desc* d, const bn::MltParams& mp, int* launches) {
+  int iters = 0;
+  const int rc = run_mlt(ctx, state(ctx), d, mp, &iters);
+  *launches = 5 * iters;
+  return rc;
+}
 
 int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector<bn::DevView>& views) {
   WfState* w = state(ctx);
@@ -239,8 +355,8 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
   const bool use_graph = !(d->flags & BN_RENDER_NO_GRAPH);
   int pool = d->queue_capacity, cap = d->block_size;  // block_size doubles as the blocks/SM cap
   if (pool <= 0 && cap <= 0 && !(d->flags & BN_RENDER_COUNT)) {  // a counting render is a one-off: no tuning
-    const bool wt = d->flags & BN_RENDER_WATERTIGHT;
-    if (w->tuned_generation != ctx->scene_generation || w->tuned_watertight != wt) {
+    const int wt = (d->flags & BN_RENDER_WATERTIGHT) ? 1 : 0;
+    if (w->tuned_generation[wt] != ctx->scene_generation) {
       // autotune on a truncated render of the same views: pool size x blocks-per-SM cap
       const int pools[5] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24};
       const int caps[2] = {0, 2};
@@ -253,15 +369,14 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
           if (rc) return rc;
           if (ms < best) {
             best = ms;
-            w->tuned_pool = pi;
-            w->tuned_cap = ci;
+            w->tuned_pool[wt] = pi;
+            w->tuned_cap[wt] = ci;
           }
         }
-      w->tuned_generation = ctx->scene_generation;
-      w->tuned_watertight = wt;
+      w->tuned_generation[wt] = ctx->scene_generation;
     }
-    pool = w->tuned_pool;
-    cap = w->tuned_cap;
+    pool = w->tuned_pool[wt];
+    cap = w->tuned_cap[wt];
   }
   if (pool <= 0) pool = 1 << 20;
   pool = std::max(pool, 1024);

@@ -8,6 +8,9 @@
 // reference seeds Sampler(x, y, frame*spp + s) and accumulates fma(1/spp, L, acc) in sample
 // order; the reduction then adds the chunks in chunk order in double precision, so the film is
 // deterministic run to run.
+//
+// kCull (BN_RENDER_CULL_SHADOW): the light sample is evaluated before its shadow ray and the ray
+// is traced only if it can change the radiance, as the wavefront does; the image is the same.
 #pragma once
 #include "dev_shading.cuh"
 #include "launch.hpp"
@@ -21,7 +24,7 @@ __device__ __forceinline__ int find_view(const long long* __restrict__ offsets, 
   return v;
 }
 
-template <bool kWT, int kWalk, int kInteg, bool kSimple = false>
+template <bool kWT, int kWalk, int kInteg, bool kSimple = false, bool kCull = false>
 __global__ void __launch_bounds__(128) k_pt_mega(DevScene s, MegaParams p) {
   constexpr bool kCount = kWalk == kWalkCount;
   // scenes walked binary are small and shading-bound: one out-of-line walk keeps the kernel in
@@ -51,7 +54,7 @@ __global__ void __launch_bounds__(128) k_pt_mega(DevScene s, MegaParams p) {
       V3 L;
       if (kInteg == BN_INTEGRATOR_NORMAL) L = li_normal<kWT, kWalk, kOutline>(s, ray, &pc);
       else if (kInteg == BN_INTEGRATOR_DIRECT) L = li_direct<kWT, kWalk, IndepSampler, kOutline>(s, ray, smp, &pc);
-      else L = li_path<kWT, false, kWalk, IndepSampler, kOutline, kSimple>(s, ray, smp, p.max_depth, p.rr_depth, &pc);
+      else L = li_path<kWT, false, kWalk, IndepSampler, kOutline, kSimple, kCull>(s, ray, smp, p.max_depth, p.rr_depth, &pc);
       acc = fma3(mk(inv_spp, inv_spp, inv_spp), L, acc);
       ++paths;
     }

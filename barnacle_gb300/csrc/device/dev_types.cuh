@@ -34,6 +34,9 @@
 namespace bn {
 
 enum : int { kPrimMesh = 0, kPrimSphere = 1 };
+// entries of a walk's stack of far nodes: a depth-64 TLAS and BLAS, the wide walk stacking up to
+// three per record level
+constexpr int kStackSize = 200;
 enum : int { kMatLambertian = 0, kMatMirror = 1, kMatDielectric = 2, kMatPBR = 3 };
 
 // Two 128-byte lines: the first holds everything a walk reads when it visits the instance (read
@@ -111,6 +114,7 @@ struct DevScene {
   int n_tri_lights;
   int light_sampler;                      // 0 uniform, 1 alias-triangles
   int n_mats;
+  int stack_cap;                          // usable stack entries (kStackSize; lower for tests)
   unsigned int* error_word;               // BN_DEVERR_* bits
 };
 

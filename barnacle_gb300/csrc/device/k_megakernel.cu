@@ -35,6 +35,7 @@ cudaError_t launch_megakernel(const DevScene& s, const MegaParams& p, cudaStream
   const long long grid = (p.n_items + bs - 1) / bs;
   if (p.integrator == BN_INTEGRATOR_NORMAL || p.integrator == BN_INTEGRATOR_DIRECT)
     return launch_megakernel_simple(s, p, st);
+  if (p.cull && !p.count) return launch_megakernel_cull(s, p, st);
   if (p.simple && !p.count && !s.wide) {
     // Lambertian meshes, uniform lights, pinhole views: the specialised path loop
     if (p.watertight) k_pt_mega<true, kWalkBinary, BN_INTEGRATOR_PATH, true><<<grid, bs, 0, st>>>(s, p);

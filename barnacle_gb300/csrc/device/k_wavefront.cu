@@ -599,7 +599,8 @@ __global__ void k_wf_control(WfParams* pp, int use_graph) {
   WfParams& p = *pp;
   int* c = p.counters;
   const bool more_work = *p.work_next < static_cast<unsigned long long>(p.total_paths);
-  bool again = c[kCntCont] > 0 || c[kCntDone] > 0 || more_work;
+  // PSSMLT chains: the chain regen counted the chains that are not finished into kCntDone
+  bool again = p.mlt ? c[kCntDone] > 0 : (c[kCntCont] > 0 || c[kCntDone] > 0 || more_work);
   const int iter = ++c[kCntIter];
   if (again && iter >= p.max_iters) {
     atomicOr(p.scene.error_word, BN_DEVERR_WATCHDOG);
@@ -637,7 +638,8 @@ int resident_grid(K kernel, int block) {
 }  // namespace
 
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st) {
-  k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
+  if (l.mlt) mlt_launch_regen(dparams, l.grid_regen, st);
+  else k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
   auto sort = [&](int shadow_queue) {
     if (!l.sort || (shadow_queue && !l.sort_shadow)) return;
     k_wf_sort_tiles<<<kScanTiles, 1024, 0, st>>>(dparams);
@@ -649,7 +651,8 @@ cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_g
     constexpr int kWalk = decltype(walk)::value;
     sort(0);
     k_wf_extend<kWT, kWalk><<<l.grid_extend, 128, 0, st>>>(dparams);
-    k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
+    if (l.mlt) mlt_launch_shade(dparams, l.grid_shade, kWT, st);
+    else k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
     sort(1);
     k_wf_shadow<kWT, kWalk><<<l.grid_shadow, 128, 0, st>>>(dparams);
   };
@@ -676,8 +679,10 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap) {
+WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
+                         bool mlt) {
   WfLaunch l{};
+  l.mlt = mlt;
   l.watertight = watertight;
   l.wide = wide;
   l.count = count;
@@ -689,13 +694,13 @@ WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return blocks_per_sm_cap > 0 ? std::min(g, sms * blocks_per_sm_cap) : g;
   };
-  l.grid_regen = cap(resident_grid(k_wf_regen, 256));
+  l.grid_regen = cap(mlt ? mlt_grid_regen() : resident_grid(k_wf_regen, 256));
   l.grid_scatter = resident_grid(k_wf_sort_scatter, 256);
   auto shape = [&](auto wt, auto walk) {
     constexpr bool kWT = decltype(wt)::value;
     constexpr int kWalk = decltype(walk)::value;
     l.grid_extend = cap(resident_grid(k_wf_extend<kWT, kWalk>, 128));
-    l.grid_shade = cap(resident_grid(k_wf_shade<kWT>, 128));
+    l.grid_shade = cap(mlt ? mlt_grid_shade(kWT) : resident_grid(k_wf_shade<kWT>, 128));
     l.grid_shadow = cap(resident_grid(k_wf_shadow<kWT, kWalk>, 128));
   };
   using WT = std::integral_constant<bool, true>;

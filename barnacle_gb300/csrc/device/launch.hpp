@@ -58,6 +58,7 @@ struct MegaParams {
   bool simple;               // Lambertian meshes, uniform light sampler, pinhole views only
   bool watertight;
   bool count;
+  bool cull;                 // trace a light sample's shadow ray only if it can change L
   float4* partial;           // n_items partial sums (scratch)
   float* film;               // concatenated views, 3 floats per pixel
   long long n_pixels;
@@ -65,6 +66,7 @@ struct MegaParams {
 };
 cudaError_t launch_megakernel(const DevScene& s, const MegaParams& p, cudaStream_t st);
 cudaError_t launch_megakernel_simple(const DevScene& s, const MegaParams& p, cudaStream_t st);  // NORMAL, DIRECT
+cudaError_t launch_megakernel_cull(const DevScene& s, const MegaParams& p, cudaStream_t st);    // PATH + cull
 cudaError_t launch_mega_reduce(const MegaParams& p, cudaStream_t st);
 
 // Film.PostProcess + Rgba32 packing over n_pixels RGB floats into 4-byte RGBA

@@ -24,6 +24,23 @@ enum : int {
   kCntSize = 16
 };
 
+// PSSMLT chains in the wavefront (WfParams::mlt): one path slot per Markov chain; the chain loop
+// of PSSMLTIntegrator.RenderSingleChain (PSSMLT.fs:275-377) advances one bounce per iteration.
+struct MltWf {
+  int n_chains, n_bootstrap, n_dims, mutations;  // mutations per chain, ceil(spp W H / chains)
+  int kelemen;                  // 1 Kelemen(eps_min, eps_max), 0 Gaussian(sigma)
+  float p_large, sigma, eps_min, eps_max;
+  float b, inv_eff_spp;         // bootstrap mean luminance, 1 / effective spp
+  const float* alias_prob;      // proportional start table, or null: uniform as the reference
+  const int* alias_idx;
+  int4* smp;                    // per chain: the MLTSampler's scalar state (MltSampler::pack)
+  float4* chain;                // 3 per chain: (L, y), (radiance, pix), (chain sampler, iteration,
+                                //   pixel of the mutation in flight, bootstrap id)
+  float4* X;                    // n_dims primary samples per chain, chain-major
+  float* film;                  // W * H * 3 FP32, splatted
+  unsigned long long* accepted;
+};
+
 struct WfParams {
   DevScene scene;
   const DevView* views;
@@ -63,6 +80,8 @@ struct WfParams {
   double* film_acc;             // 3 doubles per pixel
   float* film_out;              // 3 floats per pixel
   cudaGraphConditionalHandle cond;
+  int mlt;                      // 1: the slots hold PSSMLT chains (mlt_p), 0: camera paths
+  MltWf mlt_p;
 };
 
 struct WfLaunch {
@@ -71,9 +90,16 @@ struct WfLaunch {
   bool wide;                    // the scene's wide records (kWalkWide kernels)
   bool sort, sort_shadow;       // ray / shadow queue sorted by ray key before extend / shadow
   bool count;                   // binary walks that count their visits (BN_RENDER_COUNT)
+  bool mlt;                     // PSSMLT chains: mlt regen and shade kernels instead of regen / shade
 };
 
-WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap);
+WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
+                         bool mlt = false);
+// the chain kernels of the PSSMLT wavefront (k_mlt_wavefront.cu)
+cudaError_t mlt_launch_regen(WfParams* dparams, int grid, cudaStream_t st);
+cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, cudaStream_t st);
+int mlt_grid_regen();
+int mlt_grid_shade(bool watertight);
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
 cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st);
 

@@ -186,6 +186,10 @@ enum bn_mutation_type { BN_MUTATION_GAUSSIAN = 0, BN_MUTATION_KELEMEN = 1 };
 #define BN_RENDER_NO_GRAPH 0x4u     /* wavefront: launch the bounce loop without a CUDA graph  */
 #define BN_RENDER_COUNT 0x8u        /* count rays / BVH nodes / triangles / instances visited  */
                                     /* into bn_stats (a slower instrumented kernel variant)     */
+#define BN_RENDER_CULL_SHADOW 0x10u /* megakernel: evaluate a light sample first and trace its   */
+                                    /* shadow ray only if it can change the radiance (the same  */
+                                    /* image; the wavefront always does this, the plain form    */
+                                    /* keeps the reference's trace-then-evaluate order)          */
 
 typedef struct bn_view {
   bn_camera_desc camera;
@@ -278,19 +282,33 @@ int bn_image_write_png(const char* path, const uint8_t* rgba, int32_t width, int
 /* Render without allocating device memory (no counterpart in the reference).
  * For callers that cannot allocate during a render: a host whose device memory all comes from
  * its own arena and whose frame loop must not call cudaMalloc/cudaFree (they synchronise the
- * device), or a caller with a fixed memory budget on a shared GPU.  Same images as bn_render in
- * megakernel mode (integrator BN_INTEGRATOR_PATH, mode BN_MODE_MEGAKERNEL only), written to
- * film_device, a caller-owned DEVICE buffer of width*height*3 floats per view, views back to back
- * in Film.Pixels order.  The scene must already be uploaded (bn_scene_upload allocates; do it at
- * set-up time).  Scratch lives in one static device array of the library: 64 view records and
- * 1,048,576 partial sums (16 MiB), held by every GPU that loads the library until exit.  Limits:
- * at most 64 views and 1,048,576 pixels in total; larger renders return BN_ERR_INVALID_ARG.  The
- * first call on a device resolves the array's address (set-up): make it before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race. */
+ * device), or a caller with a fixed memory budget on a shared GPU.  It renders bn_render's
+ * megakernel mode (integrator BN_INTEGRATOR_PATH, mode BN_MODE_MEGAKERNEL only; flags
+ * BN_RENDER_WATERTIGHT and BN_RENDER_CULL_SHADOW; BN_RENDER_COUNT returns BN_ERR_UNSUPPORTED) into
+ * film_device, a caller-owned buffer of width*height*3 floats per view in DEVICE memory of the
+ * context's GPU (anything else returns BN_ERR_INVALID_ARG), views back to back in Film.Pixels
+ * order.  The context's own film (bn_film_download, bn_film_tonemap) is not written.  The scene
+ * must already be uploaded (bn_scene_upload allocates; do it at set-up time).  Scratch lives in
+ * one static device array of the library: 64 view records and 1,048,576 partial sums (16 MiB),
+ * held by every GPU that loads the library until exit.  Limits: at most 64 views and 1,048,576
+ * pixels in total; larger renders return BN_ERR_INVALID_ARG.  Images are bit-identical to
+ * bn_render's while pixels x bn_render's sample chunks per pixel fit the 1,048,576 partial sums;
+ * beyond that the call sums each pixel in fewer, longer chunks and the image equals bn_render's up
+ * to float summation order.  The first call on a device resolves the array's address (set-up):
+ * make it before any stream capture.  Calls share the array, so calls that overlap on the GPU race. */
 int bn_render_noalloc(bn_context* ctx, const bn_render_desc* desc, const bn_view* views, int32_t n_views,
                       float* film_device);
 int bn_get_stats(const bn_context* ctx, bn_stats* out);
 int bn_reset_stats(bn_context* ctx);
+
+/* Failure-detection limits (no reference counterpart; the reference's only failure path is
+ * failwith).  stack_entries caps the traversal stack a walk may use (1..200; 0 = the full 200):
+ * a walk that needs more stops and sets BN_DEVERR_STACK_OVERFLOW.  max_bounce_iterations caps the
+ * wavefront's device-side bounce loop (0 = the default cap derived from the paths and depth): a
+ * render that needs more stops and sets BN_DEVERR_WATCHDOG.  Either way the call returns
+ * BN_ERR_DEVICE and the context stays usable; tests lower them to drive those paths without
+ * faulting the GPU.  The limits hold for the context until changed. */
+int bn_set_limits(bn_context* ctx, int32_t stack_entries, int32_t max_bounce_iterations);
 
 /* ---- differentiable materials (new; no reference counterpart) --------------------------
  * A parameter vector of n_slots material slots, each

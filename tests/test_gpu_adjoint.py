@@ -3,8 +3,9 @@
 * forward with the scene's own material values and unit light scales = bn_render's image;
 * gradients against central finite differences (eps 1e-3) of the same estimator with common random
   numbers and sampling frozen at the evaluation point: within 1e-2 relative;
-* gradients against a finite-difference gradient of the CPU oracle's renderer (statistical: the
-  CPU and device random paths part by transcendental rounding);
+* gradients against a central finite difference of the CPU oracle's renderer with the same random
+  numbers (2e-2 relative per parameter; the CPU and device paths part only where transcendental
+  rounding differs);
 * the backward pass costs at most 3x the forward pass; Adam steps reduce the loss."""
 import numpy as np
 import pytest
@@ -66,32 +67,37 @@ def test_adjoint_matches_central_finite_differences(ctx, problem_small):
 
 
 def test_adjoint_agrees_with_cpu_oracle_fd(ctx, problem_small):
+    """The device adjoint against a central finite difference of the CPU oracle's renderer: both
+    evaluate the same estimator (sampling frozen at theta, the same frame id and so the same random
+    numbers), so they agree per parameter to 2e-2 relative on the 12 largest gradient entries
+    (paths where the CPU's and the device's transcendental rounding part ways are the residue)."""
     b, pb = problem_small
     ctx.upload(b)
     o = pyoracle.Scene(b.scene)
     gt = b.slot_params()
-    theta = pb.random_params(3)
+    rng = np.random.default_rng(8)
+    theta = pb.random_params(3).reshape(-1, 6)
+    theta[:, 3] = rng.uniform(0.15, 0.85, len(theta))  # clear of the alpha and metallic clamps
+    theta[:, 4] = rng.uniform(0.1, 0.9, len(theta))
+    theta = theta.reshape(-1).astype(np.float32)
+    frame = 1
     r = b.render
-    r.spp, r.max_depth, r.rr_depth, r.frame_id = 32, pb.max_depth, pb.rr_depth, 0
+    r.spp, r.max_depth, r.rr_depth, r.frame_id = 32, pb.max_depth, pb.rr_depth, frame
     v = b.views[0]
     v.width, v.height = 32, 32
     pb32 = MaterialProblem(ctx, b, width=32, height=32, spp=32)
     target = pb32.render(gt, spp=64, frame=77)
-    _, g = pb32.loss_and_grad(theta, target, frame=1)
-    # CPU oracle FD of the same loss on the same scene, common random numbers across +-eps
-    idx = np.argsort(-np.abs(g))[:6]
-    cpu = []
+    _, g = pb32.loss_and_grad(theta, target, frame=frame, sampling_params=theta)
+    idx = np.argsort(-np.abs(g))[:12]
+    eps = 5e-3
     for i in idx:
         e = np.zeros_like(theta)
-        e[i] = 2e-2
-        lp = 0.5 * ((o.render_slots(r, v, pb.n_slots, pb.emissive_base, theta + e, theta) - target) ** 2).sum()
-        lm = 0.5 * ((o.render_slots(r, v, pb.n_slots, pb.emissive_base, theta - e, theta) - target) ** 2).sum()
-        cpu.append((lp - lm) / 4e-2)
-    cpu = np.array(cpu)
-    gg = g[idx]
-    cos = float(np.dot(cpu, gg) / (np.linalg.norm(cpu) * np.linalg.norm(gg)))
-    assert cos > 0.9, (cpu, gg)
-    assert np.all(np.sign(cpu) == np.sign(gg))
+        e[i] = eps
+        xp, xm = (theta + e).astype(np.float32), (theta - e).astype(np.float32)
+        lp = 0.5 * ((o.render_slots(r, v, pb.n_slots, pb.emissive_base, xp, theta).astype(np.float64) - target) ** 2).sum()
+        lm = 0.5 * ((o.render_slots(r, v, pb.n_slots, pb.emissive_base, xm, theta).astype(np.float64) - target) ** 2).sum()
+        fd = (lp - lm) / float(xp[i] - xm[i])
+        assert abs(fd - g[i]) <= 2e-2 * abs(fd), f"param {i}: adjoint {g[i]:.6g} vs oracle FD {fd:.6g}"
 
 
 def test_adjoint_cost_within_3x_forward(ctx):

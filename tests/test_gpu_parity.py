@@ -323,15 +323,20 @@ def pixel_stats(frames):
 @pytest.mark.parametrize("name,crop,spp,frames", [("cornell", (96, 96, 160, 160), 16, 12),
                                                    ("cornell-objects", (200, 200, 264, 264), 8, 12)])
 def test_render_megakernel_statistically_matches_oracle(ctx, loaded, name, crop, spp, frames):
+    """Per-pixel means of independent device and oracle frames agree within 3 standard errors;
+    at equal spp the device's RMSE is within 2% of the oracle's, both measured against the mean of
+    the independent oracle frames, the oracle rendering the device's own frame ids (same seeds)."""
     b, o = loaded(ctx, name)
     r = b.render
     r.spp = spp
     v = b.views[0]
     x0, y0, x1, y1 = crop
-    gpu, cpu = [], []
+    gpu, cpu, cpu_same = [], [], []
     for f in range(frames):
         r.frame_id = f
         gpu.append(ctx.render(r, v)[0])
+        img, _ = o.render_pt(r, v, crop=crop)
+        cpu_same.append(img)
         r.frame_id = 1000 + f
         img, _ = o.render_pt(r, v, crop=crop)
         cpu.append(img)
@@ -345,10 +350,10 @@ def test_render_megakernel_statistically_matches_oracle(ctx, loaded, name, crop,
     valid = se > 0
     frac = (z[valid] > 3).mean()
     assert frac < 0.02, f"{frac:.3%} of pixel means differ by more than 3 standard errors"
-    # RMSE at equal spp: each estimator against the other's mean (same noise level expected)
-    rg = np.sqrt(((np.stack([g[rows, cols] for g in gpu]) - mc) ** 2).mean())
-    rc = np.sqrt(((np.stack([c[rows, cols] for c in cpu]) - mg) ** 2).mean())
-    assert abs(rg / rc - 1) < 0.1
+    # RMSE at equal spp against the independent oracle mean
+    rg = np.sqrt(((np.stack([g[rows, cols] for g in gpu]).astype(np.float64) - mc) ** 2).mean())
+    rc = np.sqrt(((np.stack([c[rows, cols] for c in cpu_same]).astype(np.float64) - mc) ** 2).mean())
+    assert abs(rg / rc - 1) < 0.02, f"RMSE {rg:.5f} (device) vs {rc:.5f} (oracle)"
 
 
 def test_render_api_errors(ctx):

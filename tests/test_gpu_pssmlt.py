@@ -102,3 +102,30 @@ def test_pssmlt_errors(ctx):
     r = mlt_desc(b, 1024, 16, 1)
     with pytest.raises(Exception):
         ctx.render(r, b.views + b.views)  # one view per PSSMLT render
+
+
+@pytest.mark.parametrize("name,kelemen,fixed,graph", [("cornell", True, False, True), ("cornell", False, True, False),
+                                                      ("cornell-objects", True, True, True)])
+def test_pssmlt_wavefront_chains_equal_lockstep(ctx, name, kelemen, fixed, graph):
+    """The chains compacted every bounce (BN_MODE_WAVEFRONT) draw every chain's random numbers in
+    the lockstep kernel's order, so each chain makes the same mutations and the same decisions:
+    the accepted count and b are identical, the films equal up to the splats' summation order."""
+    b = Bundle.generate(name, 1)
+    ctx.upload(b)
+    v = small_view(b, 64, 48)
+    r = mlt_desc(b, 1 << 14, 1024, 8, depth=8 if name == "cornell" else 12, kelemen=kelemen, fixed=fixed, frame=3)
+    out = {}
+    for mode in (capi.BN_MODE_MEGAKERNEL, capi.BN_MODE_WAVEFRONT):
+        r.mode = mode
+        r.flags = (capi.BN_RENDER_FIXED_ALIAS if fixed else 0) | (0 if graph else capi.BN_RENDER_NO_GRAPH)
+        ctx.reset_stats()
+        img = ctx.render(r, v)[0]
+        st = ctx.stats()
+        out[mode] = (img, st.accepted, st.proposed, st.bootstrap_b)
+    (a, acc_a, prop_a, b_a), (w, acc_w, prop_w, b_w) = out[capi.BN_MODE_MEGAKERNEL], out[capi.BN_MODE_WAVEFRONT]
+    assert prop_a == prop_w and b_a == b_w
+    assert acc_a == acc_w, (acc_a, acc_w)
+    ok = np.isfinite(a) & np.isfinite(w)
+    assert np.array_equal(ok, np.isfinite(a))
+    assert a[ok].sum() > 0
+    np.testing.assert_allclose(w[ok], a[ok], rtol=1e-4, atol=1e-5)

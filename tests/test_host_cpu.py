@@ -252,17 +252,36 @@ def test_json_loader_errors(tmp_path):
         Bundle.generate("no-such-workload")
 
 
-# the reference checkout next to this repository, when it is mounted (never on a GPU machine)
-CBOX = ROOT.parent / "reference" / "Asset" / "cbox.json"
-
-
-@pytest.mark.skipif(not CBOX.exists(), reason="reference asset not mounted")
 def test_json_loader_reads_reference_cbox():
+    """The reference's scene file, loaded unchanged (UTF-8 BOM, radians, thin lens, PSSMLT)."""
+    from cbox_common import CBOX
     b = Bundle.load_json(str(CBOX))
     s = b.scene.contents
     assert s.n_instances == 9 and s.n_primitives == 9
-    assert b.render.integrator == capi.BN_INTEGRATOR_PSSMLT and b.render.spp == 16
-    assert b.views[0].width == 1024 and b.views[0].height == 768
+    assert b.render.integrator == capi.BN_INTEGRATOR_PSSMLT and b.render.spp == 16 and b.render.max_depth == 8
+    assert b.render.n_chains == 1024 and b.render.n_bootstrap == 4 * 1024 * 1024
+    v = b.views[0]
+    assert v.width == 1024 and v.height == 768 and v.camera.type == capi.BN_CAM_THIN_LENS
+    assert v.camera.aperture == 4.0 and v.camera.focus_distance == 210.0
+    assert b.tone_mapping == capi.BN_TONE_ACES
+
+
+def test_oracle_render_of_cbox_matches_the_reference_sample_image():
+    """Pins the oracle to the reference's own output, coarsely: the oracle's path tracer renders
+    cbox.json (16 spp, ACES, 8-bit as Film.Save) and the 16x16 block means of the image must be
+    within the PSNR bound of the reference's "Sample - Path Tracing.png" (render settings not
+    recorded; see cbox_common.PSNR_MIN for what the bound separates)."""
+    from cbox_common import CBOX, PSNR_MIN, block_means, psnr, samples
+    b = Bundle.load_json(str(CBOX))
+    r = b.render
+    r.integrator = capi.BN_INTEGRATOR_PATH
+    r.spp = 16
+    v = b.views[0]
+    img, _ = pyoracle.Scene(b.scene).render_pt(r, v)
+    got = block_means(pyoracle.tonemap(img, capi.BN_TONE_ACES))
+    ref = samples()
+    assert psnr(got, ref["pt"]) > PSNR_MIN, psnr(got, ref["pt"])
+    assert psnr(got, ref["pssmlt"]) > PSNR_MIN, psnr(got, ref["pssmlt"])
 
 
 def test_obj_loader_fan_triangulation_and_negative_indices(tmp_path):
@@ -412,19 +431,42 @@ def test_json_loader_interpolates_keyframes_around_time_zero(tmp_path):
 
 
 def test_bench_reads_the_committed_profile_figures():
-    """bench.py reports the DRAM traffic and the L2 side of the roofline from the ncu summaries
-    under profiles/; their machine-readable lines must parse and hold plausible values."""
+    """bench.py reports the DRAM traffic per ray and the L2 side of the roofline from the
+    machine-readable ncu figures under profiles/; each must parse, carry its source and hold
+    plausible values."""
     sys_path = str(ROOT)
     import sys
     if sys_path not in sys.path:
         sys.path.insert(0, sys_path)
     import bench
 
-    traffic, l2 = bench.profile_figures("wavefront", "instances", 4)
-    assert traffic is not None and 10 ** 9 < traffic < 10 ** 13
-    assert l2["kernel"] == "k_wf_extend" and 0 < l2["hit_rate"] < 1 and 0 < l2["throughput_frac"] < 1
-    traffic, l2 = bench.profile_figures("wavefront", "instances", 8)
-    assert traffic is None  # measured at 4 spp per step only
-    _, l2 = bench.profile_figures("megakernel", "instances", 4)
-    assert l2["kernel"] == "k_pt_mega" and 0 < l2["hit_rate"] < 1
-    assert bench.profile_figures("megakernel", "cornell", 4) == (None, None)
+    prof = bench.profile_figures("instances")
+    tr = prof["traffic"]["wavefront"]
+    assert 10 < tr["dram_bytes_per_ray"] < 10 ** 5 and "ncu" in tr["source"]
+    for mode, kernel in (("wavefront", "k_wf_extend"), ("megakernel", "k_pt_mega")):
+        l2 = prof["l2"][mode]
+        assert l2["kernel"] == kernel and 0 < l2["hit_rate"] < 1 and 0 < l2["throughput_frac"] < 1
+        assert l2["source"].startswith("profiles/")
+    assert bench.profile_figures("cornell") is None
+
+
+def test_bench_cpu_tiles_cover_every_view():
+    """The CPU arms sample 16x16 tiles of every view, a different cell of a 4x4 grid per step;
+    16 steps visit every cell of every view once."""
+    import sys
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    import bench
+    from barnacle_gb300 import Bundle
+
+    b = Bundle.generate("instances", 1)  # the views live in the bundle's memory: keep it alive
+    views = b.views
+    seen = set()
+    for step in range(16):
+        tiles = bench.cpu_tiles(views, step, 1)
+        assert sorted(vi for vi, _ in tiles) == list(range(len(views)))
+        for vi, (x0, y0, x1, y1) in tiles:
+            v = views[vi]
+            assert x1 - x0 == 16 and y1 - y0 == 16 and 0 <= x0 and x1 <= v.width and 0 <= y0 and y1 <= v.height
+            seen.add((vi, x0, y0))
+    assert len(seen) == 16 * len(views)
