@@ -270,83 +270,9 @@ __device__ __forceinline__ int trav_node4(Trav& tr, const DevScene& s, Stack& st
   return kStepOk;
 }
 
-// One triangle of a BLAS leaf: its AABB pre-test (Mesh.fs:204,231), then the triangle test with
-// the current t; a hit shortens t and becomes the walk's answer.  Returns whether it hit.
-template <bool kWT, bool kCount>
-__device__ __forceinline__ bool trav_tri(Trav& tr, int j, float4 a, float4 b, float4 c, TraceCounters* cnt) {
-  if (kCount) cnt->tris++;
-  const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
-  const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
-  if (!box_hit(lo, hi, tr.orr, tr.oinv, tr.t)) return false;
-  float tt, uu, vv;
-  const bool h = kWT ? tri_wt(p0, p1, p2, tr.orr, tr.wt, tr.t, &tt, &uu, &vv)
-                     : tri_mt(p0, p1, p2, tr.orr, tr.t, &tt, &uu, &vv);
-  if (!h) return false;
-  tr.found = true;
-  tr.t = tt;
-  tr.hit.inst = tr.inst; tr.hit.tri = j; tr.hit.t = tt; tr.hit.u = uu; tr.hit.v = vv; tr.hit.sphere_root = 0;
-  return true;
-}
-
-// An instance whose world box passed (PrimitiveInstance.Intersect, Primitive.fs:111-129): the
-// ray goes to object space (direction not renormalised, so t is shared with the world ray); a
-// sphere is tested at once, a mesh's BLAS is entered when its root box passes.  Returns
-// kVisitEntered (the walk continues in the BLAS), kVisitDone (an any-hit query found a hit) or
-// kVisitMissed.  The rest of the instance's line (WorldToObject, the BLAS root's box, the
-// indices) is read in independent loads, one round trip.
-enum : int { kVisitMissed = 0, kVisitEntered = 1, kVisitDone = 2 };
-template <bool kWT, bool kWide, bool kCount>
-__device__ __forceinline__ int trav_visit_instance(Trav& tr, const DevScene& s, int k, bool any, TraceCounters* cnt) {
-  const float4* line = reinterpret_cast<const float4*>(s.inst + k);
-  float4 w2o[3];
-  w2o[0] = __ldg(line + 2); w2o[1] = __ldg(line + 3); w2o[2] = __ldg(line + 4);
-  const float4 rlo = __ldg(line + 5), rhi = __ldg(line + 6);
-  const int4 ids = __ldg(reinterpret_cast<const int4*>(line + 7));  // prim_type, node_base, tri_base, node4_root
-  tr.orr.o = xf_point(w2o, tr.wr.o);
-  tr.orr.d = xf_dir(w2o, tr.wr.d);
-  if (ids.x == kPrimSphere) {
-    float ts;
-    const int root = sphere_hit(__ldg(line + 1).w, tr.orr, tr.t, &ts);
-    if (root) {
-      tr.found = true;
-      if (any) return kVisitDone;
-      tr.t = ts;
-      tr.hit.inst = k; tr.hit.tri = 0; tr.hit.sphere_root = root; tr.hit.t = ts; tr.hit.u = 0.f; tr.hit.v = 0.f;
-    }
-    return kVisitMissed;
-  }
-  tr.oinv = inv_dir(tr.orr.d);
-  tr.ooct = octant(tr.orr.d);
-  if (kWT) tr.wt = wt_setup(tr.orr.d);
-  const int base = ids.y;
-  float te;
-  if (kWide && ids.w >= 0) {
-    // the root's box from the instance line, its record next (the root is interior)
-    if (!box_hit_t(xyz(rlo), xyz(rhi), tr.orr, tr.oinv, tr.t, &te)) return kVisitMissed;
-    tr.level = 1;
-    tr.base = base;
-    tr.tri_base = ids.z;
-    tr.inst = k;
-    tr.blas_sp0 = tr.sp;
-    tr.cur = ids.w;
-    tr.mode = kTravNode;
-    return kVisitEntered;
-  }
-  const NodeRec root = load_node(s.nodes, base);
-  if (kCount) cnt->nodes++;
-  if (!box_hit_t(root.bmin, root.bmax, tr.orr, tr.oinv, tr.t, &te)) return kVisitMissed;
-  tr.level = 1;
-  tr.base = base;
-  tr.tri_base = ids.z;
-  tr.inst = k;
-  tr.blas_sp0 = tr.sp;
-  trav_enter(tr, 0, root);
-  return kVisitEntered;
-}
-
 // one step: a wide record or a node pair, one instance (kInstRun: the leaf's instances until one
-// is entered, their boxes tested together), or kTris triangles of a leaf (0 = the rest of it);
-// returns true once the walk is finished (tr.found / tr.hit hold the answer).
+// is entered), or kTris triangles of a leaf (0 = the rest of it); returns true once the walk is
+// finished (tr.found / tr.hit hold the answer).
 // kAny: kClosest, kAnyHit, or kAnyRuntime (tr.any decides).  Every branch that exhausts its unit
 // asks for a pop, which runs once at the end of the step.
 enum : int { kClosest = 0, kAnyHit = 1, kAnyRuntime = 2 };
@@ -391,78 +317,101 @@ __device__ __forceinline__ bool trav_step(Trav& tr, const DevScene& s, Stack& st
     }
   } else if (tr.mode == kTravTri) {
     // kTris triangles of a BLAS leaf (0: the rest of the leaf): each its AABB pre-test
-    // (Mesh.fs:204,231), then the triangle test.  Triangles are fetched two at a time (their six
-    // 16-byte loads issued together) and tested in order, the second with the t the first left.
+    // (Mesh.fs:204,231), then the triangle test
     int done = 0;
 #pragma unroll 1
     while (tr.ti < tr.ti_end) {
-      const int j = tr.ti;
-      const bool two = j + 1 < tr.ti_end && (kTris <= 0 || done + 1 < kTris);
+      const int j = tr.ti++;
       const float4* tp = s.tris + 3 * (tr.tri_base + j);
-      const float4 a0 = __ldg(tp), b0 = __ldg(tp + 1), c0 = __ldg(tp + 2);
-      float4 a1 = a0, b1 = b0, c1 = c0;
-      if (two) { a1 = __ldg(tp + 3); b1 = __ldg(tp + 4); c1 = __ldg(tp + 5); }
-      if (trav_tri<kWT, kCount>(tr, j, a0, b0, c0, cnt) && any) {
-        tr.mode = kTravDone;
-        return true;
+      const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+      if (kCount) cnt->tris++;
+      const V3 p0 = xyz(a), p1 = xyz(b), p2 = xyz(c);
+      const V3 lo = min_native(min_native(p0, p1), p2), hi = max_native(max_native(p0, p1), p2);
+      if (box_hit(lo, hi, tr.orr, tr.oinv, tr.t)) {
+        float tt, uu, vv;
+        const bool h = kWT ? tri_wt(p0, p1, p2, tr.orr, tr.wt, tr.t, &tt, &uu, &vv)
+                           : tri_mt(p0, p1, p2, tr.orr, tr.t, &tt, &uu, &vv);
+        if (h) {
+          tr.found = true;
+          if (any) {
+            tr.mode = kTravDone;
+            return true;
+          }
+          tr.t = tt;
+          tr.hit.inst = tr.inst; tr.hit.tri = j; tr.hit.t = tt; tr.hit.u = uu; tr.hit.v = vv; tr.hit.sphere_root = 0;
+        }
       }
-      if (two && trav_tri<kWT, kCount>(tr, j + 1, a1, b1, c1, cnt) && any) {
-        tr.mode = kTravDone;
-        return true;
-      }
-      tr.ti = j + (two ? 2 : 1);
-      done += two ? 2 : 1;
-      if (kTris > 0 && done >= kTris) break;
+      if (kTris > 0 && ++done >= kTris) break;
     }
     pop = tr.ti >= tr.ti_end;
-  } else if (tr.mode == kTravInst && kInstRun) {
-    // the leaf's next instances (up to four, the builder's leaf size) have their world boxes
-    // tested together: the first 32 bytes of each instance's line are loaded at once, so an
-    // instance whose box fails costs no round trip of its own.  The instances are still visited
-    // in order, each box decided with the t current at its turn: t changes within the step only
-    // when a sphere instance is hit, and the boxes after it are then tested again.
-    const int i0 = tr.ii, n = min(tr.ii_end - i0, 4);
-    unsigned hm = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (j < n) {
-        const float4* line = reinterpret_cast<const float4*>(s.inst + i0 + j);
-        if (box_hit(xyz(__ldg(line)), xyz(__ldg(line + 1)), tr.wr, tr.winv, tr.t)) hm |= 1u << j;
-      }
-    }
-    const float t0 = tr.t;
-    int j = 0, visit = kVisitMissed;
-#pragma unroll 1
-    while (j < n && visit == kVisitMissed) {
-      const int k = i0 + j;
-      bool pass = (hm >> j) & 1u;
-      if (pass && tr.t != t0) {
-        const float4* line = reinterpret_cast<const float4*>(s.inst + k);
-        pass = box_hit(xyz(__ldg(line)), xyz(__ldg(line + 1)), tr.wr, tr.winv, tr.t);
-      }
-      if (kCount) cnt->insts++;
-      ++j;
-      if (pass) visit = trav_visit_instance<kWT, kWide, kCount>(tr, s, k, any, cnt);
-    }
-    tr.ii = i0 + j;
-    if (visit == kVisitDone) {
-      tr.mode = kTravDone;
-      return true;
-    }
-    pop = visit == kVisitMissed && tr.ii >= tr.ii_end;
   } else if (tr.mode == kTravInst) {
-    // the next instance of a TLAS leaf (PrimitiveInstance.Intersect, Primitive.fs:111-129)
-    const int k = tr.ii++;
-    if (kCount) cnt->insts++;
-    const float4* line = reinterpret_cast<const float4*>(s.inst + k);
-    int visit = kVisitMissed;
-    if (box_hit(xyz(__ldg(line)), xyz(__ldg(line + 1)), tr.wr, tr.winv, tr.t))
-      visit = trav_visit_instance<kWT, kWide, kCount>(tr, s, k, any, cnt);
-    if (visit == kVisitDone) {
-      tr.mode = kTravDone;
-      return true;
+    // the next instance of a TLAS leaf, or with kInstRun the leaf's instances until one is
+    // entered (PrimitiveInstance.Intersect, Primitive.fs:111-129)
+    bool entered = false;
+#pragma unroll 1
+    while (!entered && tr.ii < tr.ii_end) {
+      const int k = tr.ii++;
+      const DevInstance* I = s.inst + k;
+      if (kCount) cnt->insts++;
+      // the instance's first line in eight independent loads: bounds, WorldToObject, the BLAS
+      // root's box and the indices, so one memory round trip serves the whole visit
+      const float4* line = reinterpret_cast<const float4*>(I);
+      const float4 bmin = __ldg(line), bmax = __ldg(line + 1);
+      float4 w2o[3];
+      w2o[0] = __ldg(line + 2); w2o[1] = __ldg(line + 3); w2o[2] = __ldg(line + 4);
+      const float4 rlo = __ldg(line + 5), rhi = __ldg(line + 6);
+      const int4 ids = __ldg(reinterpret_cast<const int4*>(line + 7));  // prim_type, node_base, tri_base, node4_root
+      if (box_hit(xyz(bmin), xyz(bmax), tr.wr, tr.winv, tr.t)) {
+        tr.orr.o = xf_point(w2o, tr.wr.o);
+        tr.orr.d = xf_dir(w2o, tr.wr.d);
+        if (ids.x == kPrimSphere) {
+          float ts;
+          const int root = sphere_hit(bmax.w, tr.orr, tr.t, &ts);
+          if (root) {
+            tr.found = true;
+            if (any) {
+              tr.mode = kTravDone;
+              return true;
+            }
+            tr.t = ts;
+            tr.hit.inst = k; tr.hit.tri = 0; tr.hit.sphere_root = root; tr.hit.t = ts; tr.hit.u = 0.f; tr.hit.v = 0.f;
+          }
+        } else {
+          tr.oinv = inv_dir(tr.orr.d);
+          tr.ooct = octant(tr.orr.d);
+          if (kWT) tr.wt = wt_setup(tr.orr.d);
+          const int base = ids.y;
+          float te;
+          if (kWide && ids.w >= 0) {
+            // the root's box from the instance line, its record next (the root is interior)
+            if (box_hit_t(xyz(rlo), xyz(rhi), tr.orr, tr.oinv, tr.t, &te)) {
+              tr.level = 1;
+              tr.base = base;
+              tr.tri_base = ids.z;
+              tr.inst = k;
+              tr.blas_sp0 = tr.sp;
+              tr.cur = ids.w;
+              tr.mode = kTravNode;
+              entered = true;
+            }
+          } else {
+            const NodeRec root = load_node(s.nodes, base);
+            if (kCount) cnt->nodes++;
+            if (box_hit_t(root.bmin, root.bmax, tr.orr, tr.oinv, tr.t, &te)) {
+              tr.level = 1;
+              tr.base = base;
+              tr.tri_base = ids.z;
+              tr.inst = k;
+              tr.blas_sp0 = tr.sp;
+              trav_enter(tr, 0, root);
+              entered = true;
+            }
+          }
+        }
+      }
+      if (!kInstRun) break;
     }
-    pop = visit == kVisitMissed && tr.ii >= tr.ii_end;
+    pop = !entered && tr.ii >= tr.ii_end;
   }
   if (pop) trav_pop<kWide>(tr, s, stk);
   return tr.mode == kTravDone;

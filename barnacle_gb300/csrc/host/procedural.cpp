@@ -1,7 +1,9 @@
 // Procedural, seeded workloads: the Cornell box, the Cornell box with displaced icospheres and
 // a mirror, the 1,024-instance scene with 16 views, the PSSMLT setting, and the 32-slot
 // differentiable-material scene.  Everything is built from +,-,*,/,sqrt,floor and a
-// deterministic sine/cosine, so the same seed gives the same bits on every host.
+// deterministic sine/cosine, so the same seed gives the same bits on every host; random draws
+// are taken one per statement (or declarator), never as several arguments of one call, whose
+// evaluation order C++ leaves to the compiler.
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -358,7 +360,8 @@ void add_cornell_objects(bn_scene_bundle* b, Rng& rng, int pbr_material_override
   std::vector<int32_t> idx;
   geodesic_sphere(64, 0.05, 7u, &v, &idx);  // level 6: 81,920 triangles
   const int ico6 = b->add_mesh(std::move(v), std::move(idx));
-  const V3 bc = v3(rng.uniformf(0.2f, 0.9f), rng.uniformf(0.2f, 0.9f), rng.uniformf(0.2f, 0.9f));
+  const float br = rng.uniformf(0.2f, 0.9f), bg = rng.uniformf(0.2f, 0.9f), bb = rng.uniformf(0.2f, 0.9f);
+  const V3 bc = v3(br, bg, bb);
   const float metallic = rng.uniform() < 0.5 ? 0.f : 1.f;
   const float roughness = rng.uniformf(0.05f, 0.8f);
   int pbr = pbr_material_override >= 0 ? pbr_material_override
@@ -435,11 +438,16 @@ bool gen_instances(bn_scene_bundle* b, uint32_t seed) {
     const float x = rng.uniformf(-60.f, 60.f), z = rng.uniformf(-60.f, 60.f), y = s + rng.uniformf(0.f, 20.f);
     const int type = rng.below(4);
     int mat;
-    const V3 c = v3(rng.uniformf(0.2f, 0.9f), rng.uniformf(0.2f, 0.9f), rng.uniformf(0.2f, 0.9f));
+    const float cr = rng.uniformf(0.2f, 0.9f), cg = rng.uniformf(0.2f, 0.9f), cb = rng.uniformf(0.2f, 0.9f);
+    const V3 c = v3(cr, cg, cb);
     if (type == BN_MAT_LAMBERTIAN) mat = b->add_material(BN_MAT_LAMBERTIAN, c);
     else if (type == BN_MAT_MIRROR) mat = b->add_material(BN_MAT_MIRROR, c);
     else if (type == BN_MAT_DIELECTRIC) mat = b->add_material(BN_MAT_DIELECTRIC, v3(1, 1, 1), 1.5f);
-    else mat = b->add_material(BN_MAT_PBR, c, 1.5f, rng.uniformf(0.05f, 0.8f), rng.uniform() < 0.5 ? 0.f : 1.f);
+    else {
+      const float roughness = rng.uniformf(0.05f, 0.8f);
+      const float metallic = rng.uniform() < 0.5 ? 0.f : 1.f;
+      mat = b->add_material(BN_MAT_PBR, c, 1.5f, roughness, metallic);
+    }
     b->add_instance(blas[k], mat, -1, m4_mul(m4_mul(m4_scale(s, s, s), R), m4_translation(x, y, z)));
   }
   // 64 emissive triangles: one shared triangle mesh, 64 instances
@@ -460,7 +468,8 @@ bool gen_instances(bn_scene_bundle* b, uint32_t seed) {
     det_sincos(2.0 * 3.14159265358979323846 * (v + rng.uniform() * 0.5) / 16.0, &s, &c);
     const float rad = rng.uniformf(70.f, 95.f);
     const V3 eye = v3(static_cast<float>(c) * rad, rng.uniformf(12.f, 35.f), static_cast<float>(s) * rad);
-    const V3 target = v3(rng.uniformf(-15.f, 15.f), rng.uniformf(2.f, 10.f), rng.uniformf(-15.f, 15.f));
+    const float tx = rng.uniformf(-15.f, 15.f), ty = rng.uniformf(2.f, 10.f), tz = rng.uniformf(-15.f, 15.f);
+    const V3 target = v3(tx, ty, tz);
     b->views.push_back(make_view(look_at(eye, target, v3(0, 1, 0)), rng.uniformf(35.f, 60.f), res[k][0], res[k][1]));
   }
   b->render = default_render_desc();

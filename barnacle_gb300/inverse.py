@@ -61,17 +61,27 @@ class MaterialProblem:
 
     def adam(self, params: np.ndarray, target: np.ndarray, steps: int = 200, lr: float = 1e-2,
              beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8, frame0: int = 0):
-        """Adam with a fresh random stream per step; returns (params, [loss per step])."""
+        """Adam with a fresh random stream per step; returns (params, [loss per step]).
+
+        A step whose loss or gradient is not finite is skipped (the parameters and moments stay
+        as they were; its loss is recorded as NaN): a path can end in NaN radiance as in the
+        reference renderer (a PBR sample at a grazing direction with cos = 0 exactly makes the
+        specular term 0/0), and one such path would otherwise poison the moments for good."""
         x = self.project(np.array(params, np.float32))
         m = np.zeros_like(x, np.float64)
         v = np.zeros_like(x, np.float64)
         losses = []
+        t = 0
         for k in range(1, steps + 1):
             loss, g = self.loss_and_grad(x, target, frame=frame0 + k)
+            if not (np.isfinite(loss) and np.isfinite(g).all()):
+                losses.append(float("nan"))
+                continue
             losses.append(loss)
+            t += 1
             m = beta1 * m + (1 - beta1) * g
             v = beta2 * v + (1 - beta2) * g * g
-            mh = m / (1 - beta1 ** k)
-            vh = v / (1 - beta2 ** k)
+            mh = m / (1 - beta1 ** t)
+            vh = v / (1 - beta2 ** t)
             x = self.project((x - lr * mh / (np.sqrt(vh) + eps)).astype(np.float32))
         return x, losses

@@ -284,8 +284,11 @@ def run_extras(ctx, args, torch, flush):
         e["all"] = float(np.sqrt((d[:, :5] ** 2).mean()))
         return e
 
+    fin = [v for v in losses if np.isfinite(v)]
     out["inverse"] = {"steps": 200, "lr": 1e-2, "target_spp": 1024, "step_spp": 16, "wall_s": wall,
-                      "loss_first": losses[0], "loss_last": losses[-1],
+                      "skipped_nan_steps": len(losses) - len(fin),
+                      "loss_first": fin[0] if fin else None, "loss_last": fin[-1] if fin else None,
+                      "loss_mean_last_20": float(np.mean(fin[-20:])) if fin else None,
                       "loss_curve": [losses[k] for k in range(0, 200, 20)] + [losses[-1]],
                       "param_rmse_initial": err(x0), "param_rmse_final": err(x),
                       "workload": "materials: 32 slots, 4 emissive, 256^2, depth 8"}

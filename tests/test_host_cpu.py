@@ -470,3 +470,31 @@ def test_bench_cpu_tiles_cover_every_view():
             assert x1 - x0 == 16 and y1 - y0 == 16 and 0 <= x0 and x1 <= v.width and 0 <= y0 and y1 <= v.height
             seen.add((vi, x0, y0))
     assert len(seen) == 16 * len(views)
+
+
+def _bundle_digest(b):
+    import hashlib
+    s = b.scene.contents
+    h = hashlib.sha256()
+    for i in range(s.n_meshes):
+        m = s.meshes[i]
+        h.update(np.ctypeslib.as_array(m.vertices, shape=(m.n_vertices * 3,)).tobytes())
+        h.update(np.ctypeslib.as_array(m.indices, shape=(m.n_triangles * 3,)).tobytes())
+    for arr, n in ((s.instances, s.n_instances), (s.materials, s.n_materials), (s.lights, s.n_lights)):
+        for i in range(n):
+            h.update(bytes(arr[i]))
+    for v in b.views:
+        h.update(bytes(v))
+    return h.hexdigest()[:16]
+
+
+# the generated workloads' bits (meshes, instances, materials, lights, views), the same on every
+# host: the converged images under tests/golden/ were rendered from exactly these scenes
+WORKLOAD_DIGESTS = {"cornell": "7117cb82e4469383", "cornell-objects": "fe156941062dffd7",
+                    "instances": "6dc4b549805dc09b", "pssmlt": "4524a4473e1f2b88", "materials": "9d3871172b53493e"}
+
+
+@pytest.mark.parametrize("name", sorted(WORKLOAD_DIGESTS))
+def test_generated_workloads_have_the_same_bits_on_every_host(name):
+    b = Bundle.generate(name, 1)  # b owns the views' memory while they are hashed
+    assert _bundle_digest(b) == WORKLOAD_DIGESTS[name]
