@@ -35,6 +35,11 @@ __device__ __forceinline__ float lcg_next(uint32_t& s) {
 struct IndepSampler {
   uint32_t state;
   __device__ __forceinline__ float next() { return lcg_next(state); }
+  template <int N>
+  __device__ __forceinline__ void next_n(float* u) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) u[k] = lcg_next(state);
+  }
 };
 
 // ------------------------------------------------------------------ camera (Base/Camera.fs:12-20)
@@ -454,8 +459,10 @@ __device__ __forceinline__ bool li_bounce(const DevScene& s, PathState& ps, Smp&
   float u_sel, ulx, uly, u_lobe, ubx, uby, u_rr = 0.f;
   const int mat = hit_material(s, it);
   if (kFixed7) {
-    u_sel = smp.next(); ulx = smp.next(); uly = smp.next();
-    u_lobe = smp.next(); ubx = smp.next(); uby = smp.next(); u_rr = smp.next();
+    float u7[7];
+    smp.template next_n<7>(u7);
+    u_sel = u7[0]; ulx = u7[1]; uly = u7[2];
+    u_lobe = u7[3]; ubx = u7[4]; uby = u7[5]; u_rr = u7[6];
   }
   if (mat < 0) return true;
   if (!kFixed7) { u_sel = smp.next(); ulx = smp.next(); uly = smp.next(); }

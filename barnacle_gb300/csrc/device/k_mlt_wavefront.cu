@@ -226,8 +226,10 @@ __global__ void __launch_bounds__(128) k_mlt_shade(const WfParams* __restrict__ 
         }
         const int mat = hit_material(s, it);
         // PSSMLT.fs:201-205: seven draws per bounce whatever happens next
-        const float u_sel = m.next(), ulx = m.next(), uly = m.next();
-        const float u_lobe = m.next(), ubx = m.next(), uby = m.next(), u_rr = m.next();
+        float u7[7];
+        m.next_n<7>(u7);
+        const float u_sel = u7[0], ulx = u7[1], uly = u7[2];
+        const float u_lobe = u7[3], ubx = u7[4], uby = u7[5], u_rr = u7[6];
         if (mat < 0) {
           done = true;
         } else {

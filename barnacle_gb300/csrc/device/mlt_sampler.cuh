@@ -57,16 +57,9 @@ struct MltSampler {
     cur_iter += 1;
     index = 0;
   }
-  __device__ __forceinline__ float next() {
-    const int i = index++;
-    float4* xp = X + static_cast<long long>(min(i, max_dims - 1)) * stride;
-    float4 x;
-    if (initialized <= i) {
-      x = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
-      initialized = i + 1;
-    } else {
-      x = *xp;
-    }
+  // the draw of dimension i from its primary sample x (zeroes for a dimension drawn for the
+  // first time): EnsureReady (PSSMLT.fs:98-134), the record written back
+  __device__ __forceinline__ float draw(int i, float4 x) {
     int last_mod = __float_as_int(x.z);
     if (last_mod < last_large) {
       x.x = lcg_next(inner);
@@ -93,8 +86,37 @@ struct MltSampler {
     v = __fsub_rn(v, floorf(v));
     x.x = v;
     x.z = __int_as_float(cur_iter);
-    if (i < max_dims) *xp = x;
+    if (i < max_dims) X[static_cast<long long>(i) * stride] = x;
     return v;
+  }
+  __device__ __forceinline__ float next() {
+    const int i = index++;
+    float4 x = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
+    if (initialized <= i) initialized = i + 1;
+    else x = X[static_cast<long long>(min(i, max_dims - 1)) * stride];
+    return draw(i, x);
+  }
+  // the next N draws (Next1D N times), their primary samples loaded together first: one memory
+  // round trip instead of N dependent ones, the same values in the same order
+  template <int N>
+  __device__ __forceinline__ void next_n(float* u) {
+    const int i0 = index, init0 = initialized;
+    if (i0 + N > max_dims) {  // past the vector's end: one at a time, as Next1D
+#pragma unroll
+      for (int k = 0; k < N; ++k) u[k] = next();
+      return;
+    }
+    float4 x[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      x[k] = i0 + k < init0 ? X[static_cast<long long>(i0 + k) * stride]
+                            : make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const int i = index++;
+      if (initialized <= i) initialized = i + 1;
+      u[k] = draw(i, x[k]);
+    }
   }
   __device__ __forceinline__ void reject() {
     for (int i = 0; i < min(initialized, max_dims); ++i) {
@@ -132,11 +154,13 @@ __device__ __forceinline__ float luminance(V3 L) {
 // uPixel = Next2D * (W, H); pixel = min(W-1, int(u)); the pixel offset is u - pixel
 template <class Smp>
 __device__ __forceinline__ Ray mlt_camera(const DevView& v, Smp& smp, int* px, int* py) {
-  const float ux = __fmul_rn(smp.next(), static_cast<float>(v.width));
-  const float uy = __fmul_rn(smp.next(), static_cast<float>(v.height));
+  float u[4];
+  smp.template next_n<4>(u);
+  const float ux = __fmul_rn(u[0], static_cast<float>(v.width));
+  const float uy = __fmul_rn(u[1], static_cast<float>(v.height));
   const int x = min(v.width - 1, static_cast<int>(ux)), y = min(v.height - 1, static_cast<int>(uy));
   const float fx = __fsub_rn(ux, static_cast<float>(x)), fy = __fsub_rn(uy, static_cast<float>(y));
-  const float lx = smp.next(), ly = smp.next();
+  const float lx = u[2], ly = u[3];
   *px = x;
   *py = y;
   return camera_ray(v, x, y, fx, fy, lx, ly);

@@ -5,7 +5,8 @@ Each crop is rendered by the oracle (the CPU restatement of PathTracingIntegrato
 Extensions/Integrator/PathTracing.fs:14-81, with ProgressiveIntegrator's per-pixel seeds,
 Base/Integrator.fs:22-44) at 65,536 samples per pixel: 16 independent ranges of 4,096 samples
 (frame ids 100000..100015, far from any frame a test renders), averaged in FP64 (a range whose
-pixel is NaN is left out of that pixel's mean).
+pixel is NaN is left out of that pixel's mean).  Beside each image ("<key>:var") the per-sample
+variance of every pixel, estimated from the spread of the 16 range means.
 
     python tests/golden/make_converged.py [--threads N]
 """
@@ -68,11 +69,14 @@ def converged(o, r, v, crop, threads):
         rr.frame_id = f
         return crop_of(o.render_pt(rr, v, crop=crop, threads=1)[0], v, crop)
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        frames = list(ex.map(one, range(FRAME0, FRAME0 + RANGES)))
+        frames = np.stack(list(ex.map(one, range(FRAME0, FRAME0 + RANGES)))).astype(np.float64)
     # a path can end in NaN as in the reference (e.g. a PBR sample at a grazing wo with wo.z = 0
     # exactly: G = 0 and |wo.z| = 0 make specularBSDF 0/0, PBR.fs:47); such a range's pixel is left
-    # out of that pixel's mean, as a NaN pixel of the reference's film carries no radiance
-    return np.nanmean(np.stack(frames).astype(np.float64), 0)
+    # out of that pixel's mean, as a NaN pixel of the reference's film carries no radiance.
+    # The variance of one sample is estimated from the spread of the range means (4,096 samples
+    # each, so rare bright paths are represented in every range).
+    per_sample_var = np.nanvar(frames, 0, ddof=1) * (CONVERGED // RANGES)
+    return np.nanmean(frames, 0), per_sample_var
 
 
 def main():
@@ -88,8 +92,9 @@ def main():
         b, r = load(name)
         o = pyoracle.Scene(b.scene)
         t0 = time.time()
-        img = converged(o, r, b.views[vi], crop, args.threads)
+        img, var = converged(o, r, b.views[vi], crop, args.threads)
         out[key(name, vi, crop)] = img
+        out[key(name, vi, crop) + ":var"] = var
         print(f"{key(name, vi, crop)}: mean {img.mean():.4f}, {time.time() - t0:.1f} s", flush=True)
     np.savez_compressed(path, **out)
 

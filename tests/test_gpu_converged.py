@@ -6,7 +6,9 @@ crop of the Cornell box, of the Cornell box with objects, and of three views of 
 workload.  The device renders the crop's view FRAMES times at SPP samples per pixel:
 
 * its per-pixel means must lie within 3 standard errors of the converged image (at most 2% of the
-  values beyond), PathTracing.fs:14-81 and Integrator.fs:22-44 being the estimator both follow;
+  values beyond; the standard error from the device's frames or from the converged render's
+  per-sample variance, whichever is larger), PathTracing.fs:14-81 and Integrator.fs:22-44 being
+  the estimator both follow;
 * at equal samples per pixel its RMSE against the converged image must be within 2% of the
   oracle's own RMSE, the oracle rendering the same crop with the same frame ids (the same seeds,
   Sampler(x, y, frame * spp + s), so both estimators draw the same random numbers)."""
@@ -69,7 +71,9 @@ def bundle(name):
 @pytest.mark.parametrize("mode", [MEGA, WAVE], ids=["megakernel", "wavefront"])
 @pytest.mark.parametrize("name,vi,crop", CROPS, ids=[f"{n}-view{v}-{c[0]}-{c[1]}" for n, v, c in CROPS])
 def test_device_image_against_converged_oracle(ctx, name, vi, crop, mode):
-    conv = np.load(GOLDEN)[f"{name}:{vi}:{crop[0]},{crop[1]},{crop[2]},{crop[3]}"]
+    fx = np.load(GOLDEN)
+    key = f"{name}:{vi}:{crop[0]},{crop[1]},{crop[2]},{crop[3]}"
+    conv, var = fx[key], fx[key + ":var"]
     b, o = bundle(name)
     ctx.upload(b)
     r = b.render
@@ -88,7 +92,15 @@ def test_device_image_against_converged_oracle(ctx, name, vi, crop, mode):
     assert ok.mean() > 0.99
     n = ok.sum(0)
     gm = np.where(ok, g, 0).sum(0) / n
-    se = np.sqrt(np.where(ok, (g - gm) ** 2, 0).sum(0) / (n - 1)) / np.sqrt(n)
+    # the standard error of the device's mean: from the spread of its own frames, or from the
+    # per-sample variance of the converged render, whichever is larger.  Frames of 64 samples
+    # miss the rare bright paths (caustics through the dielectrics, glossy highlights of the
+    # small emitters) most of the time, so their spread alone understates the error of the mean
+    # for exactly the pixels those paths light; the oracle's own frames at equal spp fail the
+    # frames-only test as often as the device's (2.4-4.4 % of the values of the heavy-tailed crops).
+    se_frames = np.sqrt(np.where(ok, (g - gm) ** 2, 0).sum(0) / (n - 1)) / np.sqrt(n)
+    se_conv = np.sqrt(var / (n * SPP))
+    se = np.maximum(se_frames, se_conv)
     z = np.abs(gm - conv) / np.maximum(se, 1e-12)
     assert conv.mean() > 0.01
     frac = (z[se > 0] > 3).mean()
