@@ -240,9 +240,10 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
     return ctx->cuda_fail(e, "wavefront chain records");
   const bool wt = d->flags & BN_RENDER_WATERTIGHT;
   const bool wide = ctx->scene.wide != 0;
-  if (!w->shape.mlt || w->shape.watertight != wt || w->shape.wide != wide) {
+  const bool kelemen = mp.kelemen != 0;
+  if (!w->shape.mlt || w->shape.watertight != wt || w->shape.wide != wide || w->shape.mlt_kelemen != kelemen) {
     // 65,536 chains are few rays per launch: the queues are traversed unsorted
-    w->shape = bn::wf_launch_shape(wt, wide, false, false, false, 0, true);
+    w->shape = bn::wf_launch_shape(wt, wide, false, false, false, 0, true, kelemen);
     w->shape_cap = -1;
     if (w->exec) {
       cudaGraphExecDestroy(w->exec);

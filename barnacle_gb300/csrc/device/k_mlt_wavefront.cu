@@ -39,10 +39,13 @@ __device__ __forceinline__ int append(int* counter, bool pred) {
   return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// kKelemen: the mutation strategy fixed at compile time (1 Kelemen, 0 Gaussian), so each kernel
+// holds one strategy's code
+template <int kKelemen>
 __device__ __forceinline__ MltSampler chain_sampler(const MltWf& q, int chain) {
   MltSampler m;
   m.p_large = q.p_large;
-  m.kelemen = q.kelemen;
+  m.kelemen = kKelemen;
   m.sigma = q.sigma;
   m.eps_min = q.eps_min;
   m.eps_max = q.eps_max;
@@ -52,6 +55,7 @@ __device__ __forceinline__ MltSampler chain_sampler(const MltWf& q, int chain) {
   return m;
 }
 
+template <int kKelemen>
 __global__ void __launch_bounds__(256) k_mlt_regen(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const MltWf& q = p.mlt_p;
@@ -67,7 +71,7 @@ __global__ void __launch_bounds__(256) k_mlt_regen(const WfParams* __restrict__ 
     bool queued = valid && st.w == kChainPath;
     Splat step{-1, mk(0.f, 0.f, 0.f)}, last{-1, mk(0.f, 0.f, 0.f)};
     if (valid && (st.w == kChainFree || st.w == kChainStep)) {
-      MltSampler m = chain_sampler(q, chain);
+      MltSampler m = chain_sampler<kKelemen>(q, chain);
       float4* cr = q.chain + 3LL * chain;
       float4 c0, c1, c2;
       if (st.w == kChainFree) {
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(256) k_mlt_regen(const WfParams* __restrict__ 
   if ((threadIdx.x & 31) == 0 && a) atomicAdd(q.accepted, a);
 }
 
-template <bool kWT>
+template <bool kWT, int kKelemen>
 __global__ void __launch_bounds__(128) k_mlt_shade(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const MltWf& q = p.mlt_p;
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(128) k_mlt_shade(const WfParams* __restrict__ 
         const float4 L4 = p.bl[2 * slot + 1];
         V3 L = mk(L4.x, L4.y, L4.z);
         const int depth = st.y;
-        MltSampler m = chain_sampler(q, slot);
+        MltSampler m = chain_sampler<kKelemen>(q, slot);
         m.unpack(q.smp[slot]);
         if (__ldg(&s.inst[it.inst].light) >= 0) {
           V3 le;
@@ -295,20 +299,26 @@ int resident(K kernel, int block) {
 
 }  // namespace
 
-cudaError_t mlt_launch_regen(WfParams* dparams, int grid, cudaStream_t st) {
-  k_mlt_regen<<<grid, 256, 0, st>>>(dparams);
+cudaError_t mlt_launch_regen(WfParams* dparams, int grid, bool kelemen, cudaStream_t st) {
+  if (kelemen) k_mlt_regen<1><<<grid, 256, 0, st>>>(dparams);
+  else k_mlt_regen<0><<<grid, 256, 0, st>>>(dparams);
   return cudaGetLastError();
 }
 
-cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, cudaStream_t st) {
-  if (watertight) k_mlt_shade<true><<<grid, 128, 0, st>>>(dparams);
-  else k_mlt_shade<false><<<grid, 128, 0, st>>>(dparams);
+cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, bool kelemen, cudaStream_t st) {
+  if (watertight) {
+    if (kelemen) k_mlt_shade<true, 1><<<grid, 128, 0, st>>>(dparams);
+    else k_mlt_shade<true, 0><<<grid, 128, 0, st>>>(dparams);
+  } else {
+    if (kelemen) k_mlt_shade<false, 1><<<grid, 128, 0, st>>>(dparams);
+    else k_mlt_shade<false, 0><<<grid, 128, 0, st>>>(dparams);
+  }
   return cudaGetLastError();
 }
 
-int mlt_grid_regen() { return resident(k_mlt_regen, 256); }
+int mlt_grid_regen() { return resident(k_mlt_regen<1>, 256); }
 int mlt_grid_shade(bool watertight) {
-  return watertight ? resident(k_mlt_shade<true>, 128) : resident(k_mlt_shade<false>, 128);
+  return watertight ? resident(k_mlt_shade<true, 1>, 128) : resident(k_mlt_shade<false, 1>, 128);
 }
 
 }  // namespace bn

@@ -32,7 +32,9 @@ __global__ void __launch_bounds__(128) k_mlt_bootstrap(MltParams p) {
   p.weights[id] = luminance(L);
 }
 
-template <bool kWT, int kWalk>
+// kKelemen: the mutation strategy fixed at compile time (1 Kelemen, 0 Gaussian), so the kernel
+// holds one strategy's code
+template <bool kWT, int kWalk, int kKelemen>
 __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
   const int chain = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = chain < p.n_chains;
@@ -56,7 +58,7 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
     m.index = 0;
     m.initialized = 0;
     m.p_large = p.large_step_prob;
-    m.kelemen = p.kelemen;
+    m.kelemen = kKelemen;
     m.sigma = p.sigma;
     m.eps_min = p.eps_min;
     m.eps_max = p.eps_max;
@@ -132,7 +134,8 @@ cudaError_t launch_mlt_bootstrap(const MltParams& p, cudaStream_t st) {
 cudaError_t launch_mlt_chains(const MltParams& p, cudaStream_t st) {
   const int grid = (p.n_chains + 127) / 128;
   dispatch_walk<false>(p.scene, p.watertight, false, [&](auto wt, auto walk) {
-    k_mlt_chains<decltype(wt)::value, decltype(walk)::value><<<grid, 128, 0, st>>>(p);
+    if (p.kelemen) k_mlt_chains<decltype(wt)::value, decltype(walk)::value, 1><<<grid, 128, 0, st>>>(p);
+    else k_mlt_chains<decltype(wt)::value, decltype(walk)::value, 0><<<grid, 128, 0, st>>>(p);
   });
   return cudaGetLastError();
 }

@@ -230,12 +230,25 @@ __device__ __forceinline__ int fetch_next(int* counter, bool need) {
   return need ? base + __popc(m & ((1u << lane) - 1u)) : -1;
 }
 
+// Lanes per warp that take rays.  A queue shorter than the resident lanes (the last bounces of a
+// render, or PSSMLT's one ray per chain) is spread over every warp instead of filling the first
+// warps' 32 lanes: more warps then walk at once and hide each other's load latency, and a launch
+// ends sooner after its slowest walk.  Counting walks keep all lanes (their totals are reduced
+// over whole warps).
+template <int kWalk>
+__device__ __forceinline__ int lanes_taking_rays(int n) {
+  if (kWalk == kWalkCount) return 32;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  return min(32, max(1, (n + warps - 1) / warps));
+}
+
 template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
   const int n = p.counters[kCntActive];
   const int refill_below = p.refill_extend;
+  if ((threadIdx.x & 31) >= lanes_taking_rays<kWalk>(n)) return;
   __shared__ int2 stack_block[kWfSharedStack * 128];
   WfStack stk(stack_block);
   Trav tr;
@@ -476,6 +489,7 @@ __global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams
   const WfParams& p = *pp;
   const int n = p.counters[kCntShadow];
   const int refill_below = p.refill_shadow;
+  if ((threadIdx.x & 31) >= lanes_taking_rays<kWalk>(n)) return;
   __shared__ int2 stack_block[kWfSharedStack * 128];
   WfStack stk(stack_block);
   Trav tr;
@@ -638,7 +652,7 @@ int resident_grid(K kernel, int block) {
 }  // namespace
 
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st) {
-  if (l.mlt) mlt_launch_regen(dparams, l.grid_regen, st);
+  if (l.mlt) mlt_launch_regen(dparams, l.grid_regen, l.mlt_kelemen, st);
   else k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
   auto sort = [&](int shadow_queue) {
     if (!l.sort || (shadow_queue && !l.sort_shadow)) return;
@@ -651,7 +665,7 @@ cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_g
     constexpr int kWalk = decltype(walk)::value;
     sort(0);
     k_wf_extend<kWT, kWalk><<<l.grid_extend, 128, 0, st>>>(dparams);
-    if (l.mlt) mlt_launch_shade(dparams, l.grid_shade, kWT, st);
+    if (l.mlt) mlt_launch_shade(dparams, l.grid_shade, kWT, l.mlt_kelemen, st);
     else k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
     sort(1);
     k_wf_shadow<kWT, kWalk><<<l.grid_shadow, 128, 0, st>>>(dparams);
@@ -680,9 +694,10 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
 }
 
 WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
-                         bool mlt) {
+                         bool mlt, bool mlt_kelemen) {
   WfLaunch l{};
   l.mlt = mlt;
+  l.mlt_kelemen = mlt_kelemen;
   l.watertight = watertight;
   l.wide = wide;
   l.count = count;

@@ -91,13 +91,14 @@ struct WfLaunch {
   bool sort, sort_shadow;       // ray / shadow queue sorted by ray key before extend / shadow
   bool count;                   // binary walks that count their visits (BN_RENDER_COUNT)
   bool mlt;                     // PSSMLT chains: mlt regen and shade kernels instead of regen / shade
+  bool mlt_kelemen;             // their mutation strategy (Kelemen, else Gaussian)
 };
 
 WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
-                         bool mlt = false);
+                         bool mlt = false, bool mlt_kelemen = false);
 // the chain kernels of the PSSMLT wavefront (k_mlt_wavefront.cu)
-cudaError_t mlt_launch_regen(WfParams* dparams, int grid, cudaStream_t st);
-cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, cudaStream_t st);
+cudaError_t mlt_launch_regen(WfParams* dparams, int grid, bool kelemen, cudaStream_t st);
+cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, bool kelemen, cudaStream_t st);
 int mlt_grid_regen();
 int mlt_grid_shade(bool watertight);
 cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
