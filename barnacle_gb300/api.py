@@ -17,20 +17,23 @@ from .capi import BarnacleError, ptr
 class Bundle:
     """A library-owned scene description plus its render settings (bn_scene_bundle)."""
 
-    def __init__(self, handle: C.c_void_p):
+    def __init__(self, handle: C.c_void_p, lib: C.CDLL | None = None):
+        self._lib = lib or capi.load_library()
         self._h = handle
         self._info = capi.bn_bundle_info()
-        rc = capi.load_library().bn_bundle_info_get(self._h, C.byref(self._info))
+        rc = self._lib.bn_bundle_info_get(self._h, C.byref(self._info))
         if rc:
             raise BarnacleError(rc, capi.host_error())
 
     @classmethod
-    def generate(cls, name: str, seed: int = 1) -> "Bundle":
+    def generate(cls, name: str, seed: int = 1, lib: C.CDLL | None = None) -> "Bundle":
+        """lib: the library whose host code builds the scene (default the GPU library)."""
+        lib = lib or capi.load_library()
         h = C.c_void_p()
-        rc = capi.load_library().bn_bundle_generate(name.encode(), seed, C.byref(h))
+        rc = lib.bn_bundle_generate(name.encode(), seed, C.byref(h))
         if rc:
-            raise BarnacleError(rc, capi.host_error())
-        return cls(h)
+            raise BarnacleError(rc, f"bn_bundle_generate({name!r}) failed")
+        return cls(h, lib)
 
     @classmethod
     def load_json(cls, path: str) -> "Bundle":
@@ -42,7 +45,7 @@ class Bundle:
 
     def __del__(self):
         if getattr(self, "_h", None):
-            capi.load_library().bn_bundle_free(self._h)
+            self._lib.bn_bundle_free(self._h)
             self._h = None
 
     @property

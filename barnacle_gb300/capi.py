@@ -192,12 +192,18 @@ def load_library() -> C.CDLL:
         return _lib
     if not LIB_PATH.exists():
         raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
-    lib = C.CDLL(str(LIB_PATH))
+    _lib = bind(C.CDLL(str(LIB_PATH)))
+    return _lib
+
+
+def bind(lib: C.CDLL) -> C.CDLL:
+    """Declares the signatures of every entry point the library exports (a library built from
+    the host sources alone exports the scene and BVH helpers only)."""
     for name, (res, args) in SIGNATURES.items():
-        fn = getattr(lib, name)
-        fn.restype = res
-        fn.argtypes = args
-    _lib = lib
+        fn = getattr(lib, name, None)
+        if fn is not None:
+            fn.restype = res
+            fn.argtypes = args
     return lib
 
 

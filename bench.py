@@ -302,7 +302,8 @@ def run_reference(args, world, rank, dist):
     from barnacle_gb300 import Bundle
     from oracle import pyoracle
 
-    b = Bundle.generate(args.workload, 1)
+    # the scene from the host code alone (no GPU library is loaded by this arm)
+    b = Bundle.generate(args.workload, 1, lib=pyoracle.scenes_library())
     views = select_views(b.views, args.views)
     osc = pyoracle.Scene(b.scene)
     threads = os.cpu_count() or 1

@@ -49,6 +49,18 @@ def lib() -> C.CDLL:
     return _lib
 
 
+_scenes = None
+
+
+def scenes_library() -> C.CDLL:
+    """The host-side scene code (procedural workloads, JSON loader) built without CUDA, for the
+    CPU arms: Bundle.generate(name, seed, lib=scenes_library())."""
+    global _scenes
+    if _scenes is None:
+        _scenes = capi.bind(C.CDLL(str(_build.build_scenes())))
+    return _scenes
+
+
 def bvh_build(bounds: np.ndarray):
     b = np.ascontiguousarray(bounds, np.float32).reshape(-1, 6)
     n = len(b)

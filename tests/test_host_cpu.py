@@ -498,3 +498,10 @@ WORKLOAD_DIGESTS = {"cornell": "7117cb82e4469383", "cornell-objects": "fe1569410
 def test_generated_workloads_have_the_same_bits_on_every_host(name):
     b = Bundle.generate(name, 1)  # b owns the views' memory while they are hashed
     assert _bundle_digest(b) == WORKLOAD_DIGESTS[name]
+
+
+def test_scene_library_without_cuda_builds_the_same_scenes():
+    """The CPU arms build their scenes with the host code alone (oracle/_build/libbarnacle_scenes.so,
+    the same sources without the CUDA parts): the same bits as the GPU library's host code."""
+    b = Bundle.generate("instances", 1, lib=pyoracle.scenes_library())
+    assert _bundle_digest(b) == WORKLOAD_DIGESTS["instances"]
