@@ -26,7 +26,7 @@ struct WfState {
   int shape_cap = -1;
   // autotuned choice per uploaded scene and triangle test (index: watertight)
   long long tuned_generation[2] = {-1, -1};
-  int tuned_pool[2] = {0, 0}, tuned_cap[2] = {0, 0};
+  int tuned_pool[2] = {0, 0}, tuned_cap[2] = {0, 0}, tuned_refill[2] = {16, 16};
 
   void release() {
     DevBuf* b[] = {&params, &ray, &bl, &hit, &meta, &q_active, &q_bins, &shadow, &counters,
@@ -111,7 +111,7 @@ int build_graph(bn_context* ctx, WfState* w) {
 
 // One render (or a truncated tuning render) into w->film_acc / ctx->film.
 int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels, long long total_paths, int n_views,
-        int pool, int cap, bool use_graph, float* ms_out) {
+        int pool, int cap, int refill, bool use_graph, float* ms_out) {
   cudaError_t e;
   if ((e = ensure_pool(w, pool)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront path-state allocation");
   if ((e = w->film_acc.reserve(static_cast<size_t>(n_pixels) * 3 * sizeof(double))) != cudaSuccess)
@@ -141,10 +141,9 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   p.frame_id = d->frame_id;
   p.integrator = d->integrator;
   p.pool = pool;
-  // refill thresholds (lanes of 32 still walking), measured on the 1,024-instance workload with
-  // the mode vote: 12 / 16 / 20 / 24 / 28 give 192.9 / 193.7 / 191.6 / 187.8 / 179.5 M paths/s
-  p.refill_extend = 16;
-  p.refill_shadow = 16;
+  // refill thresholds (lanes of 32 still walking; autotuned, 16 unless told otherwise)
+  p.refill_extend = refill;
+  p.refill_shadow = refill;
   p.total_paths = total_paths;
   p.n_pixels = n_pixels;
   p.max_iters = static_cast<int>(std::min<long long>(1LL << 30, (total_paths / pool + 2) * (d->max_depth + 2) + 64));
@@ -355,18 +354,22 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
   }
   const bool use_graph = !(d->flags & BN_RENDER_NO_GRAPH);
   int pool = d->queue_capacity, cap = d->block_size;  // block_size doubles as the blocks/SM cap
+  int refill = 16;
   if (pool <= 0 && cap <= 0 && !(d->flags & BN_RENDER_COUNT)) {  // a counting render is a one-off: no tuning
     const int wt = (d->flags & BN_RENDER_WATERTIGHT) ? 1 : 0;
     if (w->tuned_generation[wt] != ctx->scene_generation) {
-      // autotune on a truncated render of the same views: pool size x blocks-per-SM cap
+      // autotune on a truncated render of the same views: pool size (the queue width) x
+      // blocks-per-SM cap, then the lanes a traversal warp refills at (the width of its batch)
       const int pools[5] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24};
       const int caps[2] = {0, 2};
+      const int refills[3] = {16, 12, 20};
       const long long sample = std::min<long long>(total, 32LL << 20);  // two fills of the largest pool
       float best = 1e30f;
+      w->tuned_refill[wt] = 16;
       for (int pi : pools)
         for (int ci : caps) {
           float ms = 0.f;
-          const int rc = run(ctx, w, d, pixels, sample, static_cast<int>(views.size()), pi, ci, use_graph, &ms);
+          const int rc = run(ctx, w, d, pixels, sample, static_cast<int>(views.size()), pi, ci, 16, use_graph, &ms);
           if (rc) return rc;
           if (ms < best) {
             best = ms;
@@ -374,14 +377,25 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
             w->tuned_cap[wt] = ci;
           }
         }
+      for (int k = 1; k < 3; ++k) {
+        float ms = 0.f;
+        const int rc = run(ctx, w, d, pixels, sample, static_cast<int>(views.size()), w->tuned_pool[wt],
+                           w->tuned_cap[wt], refills[k], use_graph, &ms);
+        if (rc) return rc;
+        if (ms < best) {
+          best = ms;
+          w->tuned_refill[wt] = refills[k];
+        }
+      }
       w->tuned_generation[wt] = ctx->scene_generation;
     }
     pool = w->tuned_pool[wt];
     cap = w->tuned_cap[wt];
+    refill = w->tuned_refill[wt];
   }
   if (pool <= 0) pool = 1 << 20;
   pool = std::max(pool, 1024);
-  const int rc = run(ctx, w, d, pixels, total, static_cast<int>(views.size()), pool, cap, use_graph, nullptr);
+  const int rc = run(ctx, w, d, pixels, total, static_cast<int>(views.size()), pool, cap, refill, use_graph, nullptr);
   if (rc) return rc;
   ctx->stats.paths += static_cast<uint64_t>(total);
   return BN_OK;
