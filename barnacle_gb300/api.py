@@ -32,7 +32,9 @@ class Bundle:
         h = C.c_void_p()
         rc = lib.bn_bundle_generate(name.encode(), seed, C.byref(h))
         if rc:
-            raise BarnacleError(rc, f"bn_bundle_generate({name!r}) failed")
+            buf = C.create_string_buffer(1024)
+            lib.bn_host_last_error(buf, 1024)
+            raise BarnacleError(rc, buf.value.decode(errors="replace"))
         return cls(h, lib)
 
     @classmethod
