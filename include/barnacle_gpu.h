@@ -175,8 +175,10 @@ enum bn_integrator_type {
                             /* and one BSDF sample that scores a light it hits                     */
 };
 enum bn_render_mode {
-  BN_MODE_MEGAKERNEL = 0, /* one thread per pixel-sample path, the plain form           */
-  BN_MODE_WAVEFRONT = 1   /* persistent queues compacted every bounce, many views/launch */
+  BN_MODE_MEGAKERNEL = 0, /* one thread per pixel-sample path (PSSMLT: per chain, in   */
+                          /* lockstep), the plain form                               */
+  BN_MODE_WAVEFRONT = 1   /* persistent queues compacted every bounce, many views per */
+                          /* launch (PSSMLT: one path slot per chain, same decisions) */
 };
 enum bn_mutation_type { BN_MUTATION_GAUSSIAN = 0, BN_MUTATION_KELEMEN = 1 };
 
@@ -198,7 +200,7 @@ typedef struct bn_view {
 
 typedef struct bn_render_desc {
   int32_t integrator;        /* bn_integrator_type                                   */
-  int32_t mode;              /* bn_render_mode (path, normal and direct integrators)  */
+  int32_t mode;              /* bn_render_mode                                        */
   int32_t spp;               /* samples per pixel, or PSSMLT mutations per pixel     */
   int32_t max_depth;         /* default 8                                            */
   int32_t rr_depth;          /* default 5                                            */
