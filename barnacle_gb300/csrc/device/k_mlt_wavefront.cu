@@ -167,7 +167,8 @@ __global__ void __launch_bounds__(256) k_mlt_regen(const WfParams* __restrict__ 
     warp_splat(q.film, step);
     warp_splat(q.film, last);
     const int qi = append(&p.counters[kCntActive], queued);
-    if (queued) p.q_active[qi] = chain;
+    if (queued && qi < p.pool) p.q_active[qi] = chain;
+    else if (queued) flag_error(p.scene, BN_DEVERR_QUEUE_OVERFLOW);
     if (valid) p.meta[chain] = st;
     // chains not finished keep the loop going (k_wf_control reads the count)
     const unsigned pending = __ballot_sync(0xffffffffu, valid && st.w != kChainDone);
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(128) k_mlt_shade(const WfParams* __restrict__ 
   const MltWf& q = p.mlt_p;
   const DevScene& s = p.scene;
   int cnt[kNumBins], total = 0;
-  for (int b = 0; b < kNumBins; ++b) { cnt[b] = p.counters[kCntBin0 + b]; total += cnt[b]; }
+  for (int b = 0; b < kNumBins; ++b) { cnt[b] = min(p.counters[kCntBin0 + b], p.pool); total += cnt[b]; }
   const int stride = gridDim.x * blockDim.x;
   const int nw = (total + 31) & ~31;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
@@ -281,6 +282,10 @@ __global__ void __launch_bounds__(128) k_mlt_shade(const WfParams* __restrict__ 
       p.meta[slot] = st;
     }
     const int si = append(&p.counters[kCntShadow], shadow);
+    if (shadow && si >= p.pool) {
+      flag_error(s, BN_DEVERR_QUEUE_OVERFLOW);
+      shadow = false;
+    }
     if (shadow) {
       float4* r = p.shadow + 4LL * si;
       r[0] = sh_o; r[1] = sh_d; r[2] = sh_a; r[3] = sh_b;

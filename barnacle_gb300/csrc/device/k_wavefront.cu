@@ -183,11 +183,14 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
       const bool active = (amask[k] >> lane) & 1u;
       const int qi = qbase + __popc(amask[k] & below);
       qbase += __popc(amask[k]);
-      if (active) p.q_active[qi] = slot[k];
+      // a queue holds at most one entry per slot; the checks only guard the buffers
+      const bool fits = qi < p.pool;
+      if (active && !fits) flag_error(p.scene, BN_DEVERR_QUEUE_OVERFLOW);
+      if (active && fits) p.q_active[qi] = slot[k];
       if (p.sort) {
         const int key = active ? p.slot_key[slot[k]] : 0;
-        if (active) p.q_key[qi] = key;
-        hist_add(p.hist, key, active);
+        if (active && fits) p.q_key[qi] = key;
+        hist_add(p.hist, key, active && fits);
       }
       if (valid[k]) p.meta[slot[k]] = m[k];
     }
@@ -246,7 +249,7 @@ template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
-  const int n = p.counters[kCntActive];
+  const int n = min(p.counters[kCntActive], p.pool);
   const int refill_below = p.refill_extend;
   if ((threadIdx.x & 31) >= lanes_taking_rays<kWalk>(n)) return;
   __shared__ int2 stack_block[kWfSharedStack * 128];
@@ -284,7 +287,9 @@ __global__ void __launch_bounds__(128, kExtendBlocks) k_wf_extend(const WfParams
         int base = 0;
         if (lane == leader) base = atomicAdd(&p.counters[kCntBin0 + bin], __popc(peers));
         base = __shfl_sync(peers, base, leader);
-        p.q_bins[static_cast<long long>(bin) * p.pool + base + __popc(peers & ((1u << lane) - 1u))] = slot;
+        const int qb = base + __popc(peers & ((1u << lane) - 1u));
+        if (qb < p.pool) p.q_bins[static_cast<long long>(bin) * p.pool + qb] = slot;
+        else flag_error(s, BN_DEVERR_QUEUE_OVERFLOW);
       }
       const int qi = fetch_next(&p.counters[kCntFetchRay], !have);
       if (!have) {
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
   const WfParams& p = *pp;
   const DevScene& s = p.scene;
   int cnt[kNumBins], total = 0;
-  for (int b = 0; b < kNumBins; ++b) { cnt[b] = p.counters[kCntBin0 + b]; total += cnt[b]; }
+  for (int b = 0; b < kNumBins; ++b) { cnt[b] = min(p.counters[kCntBin0 + b], p.pool); total += cnt[b]; }
   const int stride = gridDim.x * blockDim.x;
   const int nw = (total + 31) & ~31;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
@@ -466,7 +471,11 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
       if (done) m.w = kStatusDone;
       p.meta[slot] = m;
     }
-    const int si = warp_append(&p.counters[kCntShadow], shadow);
+    int si = warp_append(&p.counters[kCntShadow], shadow);
+    if (shadow && si >= p.pool) {
+      flag_error(s, BN_DEVERR_QUEUE_OVERFLOW);
+      shadow = false;
+    }
     if (shadow) {
       float4* r = p.shadow + 4LL * si;
       r[0] = sh_o; r[1] = sh_d; r[2] = sh_a; r[3] = sh_b;
@@ -487,7 +496,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams* __restrict__ p
 template <bool kWT, int kWalk>
 __global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams* __restrict__ pp) {
   const WfParams& p = *pp;
-  const int n = p.counters[kCntShadow];
+  const int n = min(p.counters[kCntShadow], p.pool);
   const int refill_below = p.refill_shadow;
   if ((threadIdx.x & 31) >= lanes_taking_rays<kWalk>(n)) return;
   __shared__ int2 stack_block[kWfSharedStack * 128];
@@ -591,7 +600,7 @@ __global__ void __launch_bounds__(1024) k_wf_sort_scan(const WfParams* __restric
 // per-path results do not depend on it)
 __global__ void __launch_bounds__(256) k_wf_sort_scatter(const WfParams* __restrict__ pp, int shadow_queue) {
   const WfParams& p = *pp;
-  const int n = p.counters[shadow_queue ? kCntShadow : kCntActive];
+  const int n = min(p.counters[shadow_queue ? kCntShadow : kCntActive], p.pool);
   const int* keys = shadow_queue ? p.sh_key : p.q_key;
   int* out = shadow_queue ? p.q_shadow : p.q_ray;
   const int stride = gridDim.x * blockDim.x;
