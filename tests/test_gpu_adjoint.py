@@ -4,8 +4,8 @@
 * gradients against central finite differences (eps 1e-3) of the same estimator with common random
   numbers and sampling frozen at the evaluation point: within 1e-2 relative;
 * gradients against a central finite difference of the CPU oracle's renderer with the same random
-  numbers (2e-2 relative per parameter; the CPU and device paths part only where transcendental
-  rounding differs);
+  numbers (1e-2 relative per parameter on the 12 largest entries; measured at most 5e-3; the CPU
+  and device paths part only where transcendental rounding differs);
 * the backward pass costs at most 3x the forward pass; Adam steps reduce the loss."""
 import numpy as np
 import pytest
@@ -69,7 +69,7 @@ def test_adjoint_matches_central_finite_differences(ctx, problem_small):
 def test_adjoint_agrees_with_cpu_oracle_fd(ctx, problem_small):
     """The device adjoint against a central finite difference of the CPU oracle's renderer: both
     evaluate the same estimator (sampling frozen at theta, the same frame id and so the same random
-    numbers), so they agree per parameter to 2e-2 relative on the 12 largest gradient entries
+    numbers), so they agree per parameter to 1e-2 relative on the 12 largest gradient entries
     (paths where the CPU's and the device's transcendental rounding part ways are the residue)."""
     b, pb = problem_small
     ctx.upload(b)
@@ -97,7 +97,7 @@ def test_adjoint_agrees_with_cpu_oracle_fd(ctx, problem_small):
         lp = 0.5 * ((o.render_slots(r, v, pb.n_slots, pb.emissive_base, xp, theta).astype(np.float64) - target) ** 2).sum()
         lm = 0.5 * ((o.render_slots(r, v, pb.n_slots, pb.emissive_base, xm, theta).astype(np.float64) - target) ** 2).sum()
         fd = (lp - lm) / float(xp[i] - xm[i])
-        assert abs(fd - g[i]) <= 2e-2 * abs(fd), f"param {i}: adjoint {g[i]:.6g} vs oracle FD {fd:.6g}"
+        assert abs(fd - g[i]) <= 1e-2 * abs(fd), f"param {i}: adjoint {g[i]:.6g} vs oracle FD {fd:.6g}"
 
 
 def test_adjoint_cost_within_3x_forward(ctx):

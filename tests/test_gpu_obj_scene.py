@@ -76,7 +76,7 @@ def test_obj_mesh_traces_like_the_oracle(ctx, obj_scene):
     rays["t_max"] = np.inf
     g = ctx.trace(rays)
     h, _ = o.trace(rays)
-    assert (g["instance"] >= 0).mean() > 0.5
+    assert (g["instance"] >= 0).mean() > 0.2
     assert np.array_equal(g["instance"], h["instance"]) and np.array_equal(g["primitive"], h["primitive"])
     assert np.array_equal(g["t"].view(np.uint32), h["t"].view(np.uint32))
 
