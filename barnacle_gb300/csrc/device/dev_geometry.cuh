@@ -136,8 +136,11 @@ __device__ __forceinline__ bool tri_mt(V3 p0, V3 p1, V3 p2, const Ray& r, float 
 // take the 2-D edge functions with a double-precision fallback on exact zeros, and accept the
 // hit when all edge functions share a sign.  Same t/(u, v) conventions as tri_mt.
 struct WtRay {
-  int kx, ky, kz;
+  int k;  // the permutation: kx | ky << 2 | kz << 4 (one register across the walk)
   float sx, sy, sz;
+  __device__ __forceinline__ int kx() const { return k & 3; }
+  __device__ __forceinline__ int ky() const { return (k >> 2) & 3; }
+  __device__ __forceinline__ int kz() const { return k >> 4; }
 };
 __device__ __forceinline__ WtRay wt_setup(V3 d) {
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
@@ -146,7 +149,7 @@ __device__ __forceinline__ WtRay wt_setup(V3 d) {
   int ky = kx == 2 ? 0 : kx + 1;
   if (comp(d, kz) < 0.f) { const int tmp = kx; kx = ky; ky = tmp; }
   WtRay w;
-  w.kx = kx; w.ky = ky; w.kz = kz;
+  w.k = kx | (ky << 2) | (kz << 4);
   const float dz = comp(d, kz);
   w.sx = __fdiv_rn(comp(d, kx), dz);
   w.sy = __fdiv_rn(comp(d, ky), dz);
@@ -156,10 +159,11 @@ __device__ __forceinline__ WtRay wt_setup(V3 d) {
 __device__ __forceinline__ bool tri_wt(V3 p0, V3 p1, V3 p2, const Ray& r, const WtRay& w, float tmax, float* t_out, float* u_out,
                                        float* v_out) {
   const V3 A = sub(p0, r.o), B = sub(p1, r.o), C = sub(p2, r.o);
-  const float az = comp(A, w.kz), bz = comp(B, w.kz), cz = comp(C, w.kz);
-  const float ax = __fsub_rn(comp(A, w.kx), __fmul_rn(w.sx, az)), ay = __fsub_rn(comp(A, w.ky), __fmul_rn(w.sy, az));
-  const float bx = __fsub_rn(comp(B, w.kx), __fmul_rn(w.sx, bz)), by = __fsub_rn(comp(B, w.ky), __fmul_rn(w.sy, bz));
-  const float cx = __fsub_rn(comp(C, w.kx), __fmul_rn(w.sx, cz)), cy = __fsub_rn(comp(C, w.ky), __fmul_rn(w.sy, cz));
+  const int kx = w.kx(), ky = w.ky(), kz = w.kz();
+  const float az = comp(A, kz), bz = comp(B, kz), cz = comp(C, kz);
+  const float ax = __fsub_rn(comp(A, kx), __fmul_rn(w.sx, az)), ay = __fsub_rn(comp(A, ky), __fmul_rn(w.sy, az));
+  const float bx = __fsub_rn(comp(B, kx), __fmul_rn(w.sx, bz)), by = __fsub_rn(comp(B, ky), __fmul_rn(w.sy, bz));
+  const float cx = __fsub_rn(comp(C, kx), __fmul_rn(w.sx, cz)), cy = __fsub_rn(comp(C, ky), __fmul_rn(w.sy, cz));
   float U = __fsub_rn(__fmul_rn(cx, by), __fmul_rn(cy, bx));
   float V = __fsub_rn(__fmul_rn(ax, cy), __fmul_rn(ay, cx));
   float W = __fsub_rn(__fmul_rn(bx, ay), __fmul_rn(by, ax));
