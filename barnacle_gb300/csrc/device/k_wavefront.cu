@@ -115,13 +115,33 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
 #pragma unroll
     for (int k = 0; k < kRegenRows; ++k)
       if (valid[k] && m[k].w == kStatusDone) L[k] = p.bl[2 * slot[k] + 1];
+    // lanes of a row that retire paths of the same pixel (samples of one pixel are claimed
+    // together) add their terms in double and share one set of atomics
 #pragma unroll
     for (int k = 0; k < kRegenRows; ++k) {
-      if (valid[k] && m[k].w == kStatusDone) {
-        double* f = p.film_acc + 3LL * m[k].x;
-        atomicAdd(f, static_cast<double>(__fmul_rn(L[k].x, inv_spp)));
-        atomicAdd(f + 1, static_cast<double>(__fmul_rn(L[k].y, inv_spp)));
-        atomicAdd(f + 2, static_cast<double>(__fmul_rn(L[k].z, inv_spp)));
+      const bool retire = valid[k] && m[k].w == kStatusDone;
+      const unsigned peers = __match_any_sync(0xffffffffu, retire ? m[k].x : -1);
+      if (retire) {
+        double r = static_cast<double>(__fmul_rn(L[k].x, inv_spp));
+        double g = static_cast<double>(__fmul_rn(L[k].y, inv_spp));
+        double b = static_cast<double>(__fmul_rn(L[k].z, inv_spp));
+        const int leader = __ffs(peers) - 1;
+        if (__popc(peers) > 1) {
+          double sr = 0.0, sg = 0.0, sb = 0.0;
+          for (unsigned q = peers; q; q &= q - 1) {
+            const int src = __ffs(q) - 1;
+            sr += __shfl_sync(peers, r, src);
+            sg += __shfl_sync(peers, g, src);
+            sb += __shfl_sync(peers, b, src);
+          }
+          r = sr; g = sg; b = sb;
+        }
+        if (lane == leader) {
+          double* f = p.film_acc + 3LL * m[k].x;
+          atomicAdd(f, r);
+          atomicAdd(f + 1, g);
+          atomicAdd(f + 2, b);
+        }
         m[k].w = kStatusFree;
       }
     }
@@ -144,10 +164,11 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
         if (!((wmask[k] >> lane) & 1u) || id >= p.total_paths) continue;
         const int vi = find_view(p, id);
         const DevView& v = p.views[vi];
+        // path ids run over the samples of a pixel first, so a warp's claims are mostly the
+        // samples of one pixel (their retirements share atomics, see above)
         const long long local = id - v.path_offset;
-        const long long npix = static_cast<long long>(v.width) * v.height;
-        const int sid = static_cast<int>(local / npix);
-        const long long pix = local - sid * npix;
+        const long long pix = local / p.spp;
+        const int sid = static_cast<int>(local - pix * p.spp);
         const int x = static_cast<int>(pix % v.width), y = static_cast<int>(pix / v.width);
         IndepSampler smp{xxhash32_three(static_cast<uint32_t>(x), static_cast<uint32_t>(y),
                                         static_cast<uint32_t>(p.frame_id * p.spp + sid))};
