@@ -115,33 +115,15 @@ __global__ void __launch_bounds__(256) k_wf_regen(const WfParams* __restrict__ p
 #pragma unroll
     for (int k = 0; k < kRegenRows; ++k)
       if (valid[k] && m[k].w == kStatusDone) L[k] = p.bl[2 * slot[k] + 1];
-    // lanes of a row that retire paths of the same pixel (samples of one pixel are claimed
-    // together) add their terms in double and share one set of atomics
+    // (lanes retiring samples of the same pixel could first sum in a warp and share one set of
+    // atomics; measured 0.5% slower than one set per lane on the instanced workload)
 #pragma unroll
     for (int k = 0; k < kRegenRows; ++k) {
-      const bool retire = valid[k] && m[k].w == kStatusDone;
-      const unsigned peers = __match_any_sync(0xffffffffu, retire ? m[k].x : -1);
-      if (retire) {
-        double r = static_cast<double>(__fmul_rn(L[k].x, inv_spp));
-        double g = static_cast<double>(__fmul_rn(L[k].y, inv_spp));
-        double b = static_cast<double>(__fmul_rn(L[k].z, inv_spp));
-        const int leader = __ffs(peers) - 1;
-        if (__popc(peers) > 1) {
-          double sr = 0.0, sg = 0.0, sb = 0.0;
-          for (unsigned q = peers; q; q &= q - 1) {
-            const int src = __ffs(q) - 1;
-            sr += __shfl_sync(peers, r, src);
-            sg += __shfl_sync(peers, g, src);
-            sb += __shfl_sync(peers, b, src);
-          }
-          r = sr; g = sg; b = sb;
-        }
-        if (lane == leader) {
-          double* f = p.film_acc + 3LL * m[k].x;
-          atomicAdd(f, r);
-          atomicAdd(f + 1, g);
-          atomicAdd(f + 2, b);
-        }
+      if (valid[k] && m[k].w == kStatusDone) {
+        double* f = p.film_acc + 3LL * m[k].x;
+        atomicAdd(f, static_cast<double>(__fmul_rn(L[k].x, inv_spp)));
+        atomicAdd(f + 1, static_cast<double>(__fmul_rn(L[k].y, inv_spp)));
+        atomicAdd(f + 2, static_cast<double>(__fmul_rn(L[k].z, inv_spp)));
         m[k].w = kStatusFree;
       }
     }
