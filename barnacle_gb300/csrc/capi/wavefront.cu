@@ -27,6 +27,16 @@ struct WfState {
   // autotuned choice per uploaded scene and triangle test (index: watertight)
   long long tuned_generation[2] = {-1, -1};
   int tuned_pool[2] = {0, 0}, tuned_cap[2] = {0, 0}, tuned_refill[2] = {16, 16};
+  // the PSSMLT iteration's second stream and its fork / join events (made on first use)
+  bn::WfFork fork{nullptr, nullptr, nullptr};
+
+  cudaError_t ensure_fork() {
+    cudaError_t e = cudaSuccess;
+    if (!fork.side) e = cudaStreamCreateWithFlags(&fork.side, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !fork.fork) e = cudaEventCreateWithFlags(&fork.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess && !fork.join) e = cudaEventCreateWithFlags(&fork.join, cudaEventDisableTiming);
+    return e;
+  }
 
   void release() {
     DevBuf* b[] = {&params, &ray, &bl, &hit, &meta, &q_active, &q_bins, &shadow, &counters,
@@ -37,6 +47,10 @@ struct WfState {
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
     graph = nullptr;
+    if (fork.fork) cudaEventDestroy(fork.fork);
+    if (fork.join) cudaEventDestroy(fork.join);
+    if (fork.side) cudaStreamDestroy(fork.side);
+    fork = bn::WfFork{nullptr, nullptr, nullptr};
   }
 };
 
@@ -74,7 +88,8 @@ cudaError_t ensure_pool(WfState* w, int pool) {
   return cudaSuccess;
 }
 
-// the while-node graph: body = one iteration (regen, extend, shade, shadow, control)
+// the while-node graph: body = one iteration (regen, extend, shade, shadow, control; for PSSMLT
+// chains shadow and extend as two branches, then shade, regen, control)
 int build_graph(bn_context* ctx, WfState* w) {
   if (w->exec) {
     cudaGraphExecDestroy(w->exec);
@@ -100,7 +115,8 @@ int build_graph(bn_context* ctx, WfState* w) {
   if ((e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
       cudaSuccess)
     return ctx->cuda_fail(e, "cudaStreamBeginCaptureToGraph");
-  cudaError_t le = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, true, ctx->stream);
+  cudaError_t le = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, true, ctx->stream,
+                                           w->shape.mlt ? &w->fork : nullptr);
   cudaGraph_t captured = body;
   e = cudaStreamEndCapture(ctx->stream, &captured);
   if (le != cudaSuccess) return ctx->cuda_fail(le, "capture of the bounce loop");
@@ -234,6 +250,7 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
   cudaError_t e;
   const int pool = mp.n_chains;
   if ((e = ensure_pool(w, pool)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront chain-state allocation");
+  if ((e = w->ensure_fork()) != cudaSuccess) return ctx->cuda_fail(e, "wavefront chain stream");
   if ((e = w->mlt_smp.reserve(static_cast<size_t>(pool) * sizeof(int4))) != cudaSuccess ||
       (e = w->mlt_chain.reserve(static_cast<size_t>(pool) * 3 * sizeof(float4))) != cudaSuccess)
     return ctx->cuda_fail(e, "wavefront chain records");
@@ -264,9 +281,10 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
   p.refill_shadow = 16;
   p.total_paths = 0;
   p.n_pixels = 0;
-  // a mutation's path takes at most max_depth iterations (at least one)
+  // a mutation's path takes at most max_depth iterations (at least one), and one more when its
+  // last shadow record is traced after it ends
   p.max_iters = static_cast<int>(std::min<long long>(
-      1LL << 30, (static_cast<long long>(mp.mutations_per_chain) + 1) * std::max(1, d->max_depth) + 64));
+      1LL << 30, (static_cast<long long>(mp.mutations_per_chain) + 1) * (std::max(1, d->max_depth) + 1) + 64));
   if (ctx->limit_iters > 0) p.max_iters = ctx->limit_iters;
   p.ray = w->ray.as<float4>();
   p.bl = w->bl.as<float4>();
@@ -318,7 +336,7 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
     if ((e = cudaGraphLaunch(w->exec, st)) != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphLaunch");
   } else {
     for (int it = 0; it < p.max_iters + 1; ++it) {
-      if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st)) != cudaSuccess)
+      if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st, &w->fork)) != cudaSuccess)
         return ctx->cuda_fail(e, "wavefront chain iteration launch");
       int again = 0;
       cudaMemcpyAsync(&again, w->counters.as<int>() + bn::kCntAgain, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -2,20 +2,23 @@
 // PSSMLT.fs:275-377, with PSSMLTIntegrator.Li, :172-245, one bounce per iteration).
 //
 // One path slot per Markov chain.  An iteration of the bounce loop is
-//   mlt regen   every chain whose path has ended takes its Metropolis step (acceptance, the
-//               expected-value splats, Accept/Reject of the primary samples) and starts its next
-//               mutation (StartIteration, the pixel and lens draws, the camera ray); chains whose
-//               path goes on are queued as they are.  A chain that has run all its mutations
-//               splats its last state and stops.
-//   extend      closest hit for the queue (the path tracer's persistent traversal kernel)
+//   shadow      any hit for the shadow records of the last iteration's bounce (the path tracer's
+//   + extend    kernels), on a second stream alongside the closest hit for the rays queued by the
+//               last iteration: a bounce waits for one walk instead of two in a row
 //   mlt shade   PSSMLTIntegrator.Li's bounce with its fixed 7 draws from the chain's MLTSampler:
 //               emission with MIS, a shadow record for the light sample when it can change the
 //               radiance, the BSDF sample, Russian roulette
-//   shadow      any hit for the shadow records (the path tracer's kernel)
-//   control     another iteration while any chain still has a path queued.
+//   mlt regen   every chain whose path has ended (and whose last shadow record has been traced)
+//               takes its Metropolis step (acceptance, the expected-value splats, Accept/Reject
+//               of the primary samples) and starts its next mutation (StartIteration, the pixel and
+//               lens draws, the camera ray); chains whose path goes on are queued as they are.  A
+//               chain that has run all its mutations splats its last state and stops.
+//   control     moves the queues filled this iteration into place; another iteration while any
+//               chain is not finished.
 // A chain whose path is short starts its next mutation at once instead of waiting for the
 // longest path of its warp, and every traversal runs compacted and binned by material.  Each
-// chain draws exactly the random numbers of the lockstep kernel (k_mlt_chains) in the same order,
+// chain draws exactly the random numbers of the lockstep kernel (k_mlt_chains) in the same order
+// and adds its path's terms to L in the same order (a bounce's emission, then its shadow term),
 // so both forms give every chain the same mutations and decisions; only the film's summation
 // order differs.  Primary samples are chain-major here: the 7 draws of a bounce read one chain's
 // consecutive 16-byte records, which a lane fetches in a few sectors whatever its neighbours do.
@@ -26,7 +29,9 @@
 namespace bn {
 namespace {
 
-constexpr int kChainFree = 0, kChainPath = 1, kChainStep = 2, kChainDone = 3;
+// kChainWait: the path ended with a shadow record not yet traced; the chain steps one iteration
+// later
+constexpr int kChainFree = 0, kChainPath = 1, kChainStep = 2, kChainDone = 3, kChainWait = 4;
 constexpr int kBinMiss = 4;
 
 __device__ __forceinline__ int append(int* counter, bool pred) {
@@ -166,7 +171,9 @@ __global__ void __launch_bounds__(256) k_mlt_regen(const WfParams* __restrict__ 
     }
     warp_splat(q.film, step);
     warp_splat(q.film, last);
-    const int qi = append(&p.counters[kCntActive], queued);
+    // the shadow record of a waiting chain is traced in the next iteration: it steps in the one after
+    if (valid && st.w == kChainWait) st.w = kChainStep;
+    const int qi = append(&p.counters[kCntActiveNext], queued);
     if (queued && qi < p.pool) p.q_active[qi] = chain;
     else if (queued) flag_error(p.scene, BN_DEVERR_QUEUE_OVERFLOW);
     if (valid) p.meta[chain] = st;
@@ -278,10 +285,10 @@ __global__ void __launch_bounds__(128) k_mlt_shade(const WfParams* __restrict__ 
         p.bl[2 * slot + 1] = make_float4(L.x, L.y, L.z, 0.f);
         q.smp[slot] = m.pack();
       }
-      st.w = done ? kChainStep : kChainPath;
+      st.w = done ? (shadow ? kChainWait : kChainStep) : kChainPath;
       p.meta[slot] = st;
     }
-    const int si = append(&p.counters[kCntShadow], shadow);
+    const int si = append(&p.counters[kCntShadowNext], shadow);
     if (shadow && si >= p.pool) {
       flag_error(s, BN_DEVERR_QUEUE_OVERFLOW);
       shadow = false;

@@ -38,6 +38,8 @@ constexpr int kWfTris = 4;
 constexpr bool kWfInstRun = true;
 // blocks of 128 per SM the traversal kernels are compiled for (registers: 65,536 / (128 x blocks))
 constexpr int kExtendBlocks = 7, kShadowBlocks = 8;
+// and per SM when the PSSMLT chains trace both queues at once
+constexpr int kMltExtendBlocks = 3, kMltShadowBlocks = 4;
 // stack entries per lane kept in shared memory (8 bytes each, x 128 lanes per block)
 constexpr int kWfSharedStack = 16;
 using WfStack = SharedStack<kWfSharedStack, 128>;
@@ -632,8 +634,16 @@ __global__ void k_wf_control(WfParams* pp, int use_graph) {
     atomicOr(p.scene.error_word, BN_DEVERR_WATCHDOG);
     again = false;
   }
-  c[kCntActive] = 0;
-  c[kCntShadow] = 0;
+  if (p.mlt) {
+    // the chains' queues were filled this iteration for the next one
+    c[kCntActive] = c[kCntActiveNext];
+    c[kCntShadow] = c[kCntShadowNext];
+    c[kCntActiveNext] = 0;
+    c[kCntShadowNext] = 0;
+  } else {
+    c[kCntActive] = 0;
+    c[kCntShadow] = 0;
+  }
   c[kCntFetchRay] = 0;
   c[kCntFetchShadow] = 0;
   c[kCntCont] = 0;
@@ -663,22 +673,40 @@ int resident_grid(K kernel, int block) {
 
 }  // namespace
 
-cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st) {
-  if (l.mlt) mlt_launch_regen(dparams, l.grid_regen, l.mlt_kelemen, st);
-  else k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
+cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st,
+                                const WfFork* fk) {
   auto sort = [&](int shadow_queue) {
     if (!l.sort || (shadow_queue && !l.sort_shadow)) return;
     k_wf_sort_tiles<<<kScanTiles, 1024, 0, st>>>(dparams);
     k_wf_sort_scan<<<kScanTiles, 1024, 0, st>>>(dparams);
     k_wf_sort_scatter<<<l.grid_scatter, 256, 0, st>>>(dparams, shadow_queue);
   };
+  cudaError_t e = cudaSuccess;
   auto go = [&](auto wt, auto walk) {
     constexpr bool kWT = decltype(wt)::value;
     constexpr int kWalk = decltype(walk)::value;
+    if (l.mlt) {
+      // PSSMLT chains: the shadow records of the last bounce are traced while the rays of the
+      // next one are (they touch different fields of a slot: the shadow kernel adds to L, the
+      // extension writes the hit), then shade, then the chains' Metropolis steps
+      if (fk) {
+        if ((e = cudaEventRecord(fk->fork, st)) != cudaSuccess) return;
+        if ((e = cudaStreamWaitEvent(fk->side, fk->fork, 0)) != cudaSuccess) return;
+      }
+      k_wf_shadow<kWT, kWalk><<<l.grid_shadow, 128, 0, fk ? fk->side : st>>>(dparams);
+      k_wf_extend<kWT, kWalk><<<l.grid_extend, 128, 0, st>>>(dparams);
+      if (fk) {
+        if ((e = cudaEventRecord(fk->join, fk->side)) != cudaSuccess) return;
+        if ((e = cudaStreamWaitEvent(st, fk->join, 0)) != cudaSuccess) return;
+      }
+      mlt_launch_shade(dparams, l.grid_shade, kWT, l.mlt_kelemen, st);
+      mlt_launch_regen(dparams, l.grid_regen, l.mlt_kelemen, st);
+      return;
+    }
+    k_wf_regen<<<l.grid_regen, 256, 0, st>>>(dparams);
     sort(0);
     k_wf_extend<kWT, kWalk><<<l.grid_extend, 128, 0, st>>>(dparams);
-    if (l.mlt) mlt_launch_shade(dparams, l.grid_shade, kWT, l.mlt_kelemen, st);
-    else k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
+    k_wf_shade<kWT><<<l.grid_shade, 128, 0, st>>>(dparams);
     sort(1);
     k_wf_shadow<kWT, kWalk><<<l.grid_shadow, 128, 0, st>>>(dparams);
   };
@@ -696,6 +724,7 @@ cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_g
     else if (l.wide) go(MT{}, Wide{});
     else go(MT{}, Bin{});
   }
+  if (e != cudaSuccess) return e;
   k_wf_control<<<1, 1, 0, st>>>(dparams, use_graph ? 1 : 0);
   return cudaGetLastError();
 }
@@ -715,12 +744,13 @@ WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow
   l.count = count;
   l.sort = sort;
   l.sort_shadow = sort && sort_shadow;
-  auto cap = [&](int g) {
-    int sms = 0, dev = 0;
+  auto sms = [] {
+    int n = 0, dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return blocks_per_sm_cap > 0 ? std::min(g, sms * blocks_per_sm_cap) : g;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
   };
+  auto cap = [&](int g) { return blocks_per_sm_cap > 0 ? std::min(g, sms() * blocks_per_sm_cap) : g; };
   l.grid_regen = cap(mlt ? mlt_grid_regen() : resident_grid(k_wf_regen, 256));
   l.grid_scatter = resident_grid(k_wf_sort_scatter, 256);
   auto shape = [&](auto wt, auto walk) {
@@ -729,6 +759,12 @@ WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow
     l.grid_extend = cap(resident_grid(k_wf_extend<kWT, kWalk>, 128));
     l.grid_shade = cap(mlt ? mlt_grid_shade(kWT) : resident_grid(k_wf_shade<kWT>, 128));
     l.grid_shadow = cap(resident_grid(k_wf_shadow<kWT, kWalk>, 128));
+    if (mlt) {
+      // the two traversals run side by side: each takes part of every SM (registers: 3 x 128 x
+      // 72 + 4 x 128 x 64 = 60,416 of 65,536), enough lanes for the chains' one ray each
+      l.grid_extend = std::min(l.grid_extend, sms() * kMltExtendBlocks);
+      l.grid_shadow = std::min(l.grid_shadow, sms() * kMltShadowBlocks);
+    }
   };
   using WT = std::integral_constant<bool, true>;
   using MT = std::integral_constant<bool, false>;

@@ -21,6 +21,10 @@ enum : int {
   kCntFetchRay = 6, // dynamic-fetch cursors of the extend and shadow kernels
   kCntFetchShadow = 7,
   kCntBin0 = 8,     // 8..13: per-bin hit counts
+  // PSSMLT chains: the queues filled in one iteration and traced in the next (k_wf_control moves
+  // them into kCntActive / kCntShadow)
+  kCntShadowNext = 14,
+  kCntActiveNext = 15,
   kCntSize = 16
 };
 
@@ -101,7 +105,14 @@ cudaError_t mlt_launch_regen(WfParams* dparams, int grid, bool kelemen, cudaStre
 cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, bool kelemen, cudaStream_t st);
 int mlt_grid_regen();
 int mlt_grid_shade(bool watertight);
-cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st);
+// a second stream and two events: the PSSMLT iteration traces its shadow and extension rays on
+// two streams at once (fork / join, also inside a graph capture)
+struct WfFork {
+  cudaStream_t side;
+  cudaEvent_t fork, join;
+};
+cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_graph, cudaStream_t st,
+                                const WfFork* fk = nullptr);
 cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st);
 
 }  // namespace bn
