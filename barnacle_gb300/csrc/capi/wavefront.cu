@@ -257,9 +257,11 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
   const bool wt = d->flags & BN_RENDER_WATERTIGHT;
   const bool wide = ctx->scene.wide != 0;
   const bool kelemen = mp.kelemen != 0;
-  if (!w->shape.mlt || w->shape.watertight != wt || w->shape.wide != wide || w->shape.mlt_kelemen != kelemen) {
-    // 65,536 chains are few rays per launch: the queues are traversed unsorted
-    w->shape = bn::wf_launch_shape(wt, wide, false, false, false, 0, true, kelemen);
+  // 65,536 chains are few rays per launch: the queues are traversed unsorted
+  const bn::WfLaunch want = bn::wf_launch_shape(wt, wide, false, false, false, 0, true, kelemen, pool);
+  if (!w->shape.mlt || w->shape.watertight != wt || w->shape.wide != wide || w->shape.mlt_kelemen != kelemen ||
+      w->shape.grid_extend != want.grid_extend || w->shape.grid_shadow != want.grid_shadow) {
+    w->shape = want;
     w->shape_cap = -1;
     if (w->exec) {
       cudaGraphExecDestroy(w->exec);

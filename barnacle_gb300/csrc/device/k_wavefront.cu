@@ -38,8 +38,6 @@ constexpr int kWfTris = 4;
 constexpr bool kWfInstRun = true;
 // blocks of 128 per SM the traversal kernels are compiled for (registers: 65,536 / (128 x blocks))
 constexpr int kExtendBlocks = 7, kShadowBlocks = 8;
-// and per SM when the PSSMLT chains trace both queues at once
-constexpr int kMltExtendBlocks = 3, kMltShadowBlocks = 4;
 // stack entries per lane kept in shared memory (8 bytes each, x 128 lanes per block)
 constexpr int kWfSharedStack = 16;
 using WfStack = SharedStack<kWfSharedStack, 128>;
@@ -735,7 +733,7 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
 }
 
 WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
-                         bool mlt, bool mlt_kelemen) {
+                         bool mlt, bool mlt_kelemen, long long mlt_chains) {
   WfLaunch l{};
   l.mlt = mlt;
   l.mlt_kelemen = mlt_kelemen;
@@ -759,11 +757,13 @@ WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow
     l.grid_extend = cap(resident_grid(k_wf_extend<kWT, kWalk>, 128));
     l.grid_shade = cap(mlt ? mlt_grid_shade(kWT) : resident_grid(k_wf_shade<kWT>, 128));
     l.grid_shadow = cap(resident_grid(k_wf_shadow<kWT, kWalk>, 128));
-    if (mlt) {
-      // the two traversals run side by side: each takes part of every SM (registers: 3 x 128 x
-      // 72 + 4 x 128 x 64 = 60,416 of 65,536), enough lanes for the chains' one ray each
-      l.grid_extend = std::min(l.grid_extend, sms() * kMltExtendBlocks);
-      l.grid_shadow = std::min(l.grid_shadow, sms() * kMltShadowBlocks);
+    if (mlt_chains > 0) {
+      // the two traversals run side by side, each with one lane per chain (a queue holds at most
+      // one ray per chain): for 65,536 chains 512 blocks each, 512 x 128 x (72 + 64) registers,
+      // 90 % of the SMs' together
+      const int blocks = static_cast<int>(std::min<long long>((mlt_chains + 127) / 128, 1 << 30));
+      l.grid_extend = std::min(l.grid_extend, blocks);
+      l.grid_shadow = std::min(l.grid_shadow, blocks);
     }
   };
   using WT = std::integral_constant<bool, true>;

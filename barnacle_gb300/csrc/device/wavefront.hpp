@@ -98,8 +98,9 @@ struct WfLaunch {
   bool mlt_kelemen;             // their mutation strategy (Kelemen, else Gaussian)
 };
 
+// mlt_chains: PSSMLT chains (one slot each); sizes the traversal grids so both fit side by side
 WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
-                         bool mlt = false, bool mlt_kelemen = false);
+                         bool mlt = false, bool mlt_kelemen = false, long long mlt_chains = 0);
 // the chain kernels of the PSSMLT wavefront (k_mlt_wavefront.cu)
 cudaError_t mlt_launch_regen(WfParams* dparams, int grid, bool kelemen, cudaStream_t st);
 cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, bool kelemen, cudaStream_t st);

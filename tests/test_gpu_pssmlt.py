@@ -129,3 +129,28 @@ def test_pssmlt_wavefront_chains_equal_lockstep(ctx, name, kelemen, fixed, graph
     assert np.array_equal(ok, np.isfinite(a))
     assert a[ok].sum() > 0
     np.testing.assert_allclose(w[ok], a[ok], rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize("depth,graph", [(1, True), (1, False), (2, True)])
+def test_pssmlt_wavefront_short_paths_equal_lockstep(ctx, depth, graph):
+    """Paths of one or two bounces: at depth 1 every path ends at its first bounce, most with a
+    shadow record still to trace, so nearly every chain waits an iteration before its Metropolis
+    step; the decisions must still be the lockstep kernel's."""
+    b = Bundle.generate("cornell-objects", 1)
+    ctx.upload(b)
+    v = small_view(b, 64, 48)
+    r = mlt_desc(b, 1 << 14, 1024, 8, depth=depth, frame=5)
+    out = {}
+    for mode in (capi.BN_MODE_MEGAKERNEL, capi.BN_MODE_WAVEFRONT):
+        r.mode = mode
+        r.flags = 0 if graph else capi.BN_RENDER_NO_GRAPH
+        ctx.reset_stats()
+        img = ctx.render(r, v)[0]
+        st = ctx.stats()
+        out[mode] = (img, st.accepted, st.proposed, st.bootstrap_b)
+    (a, acc_a, prop_a, b_a), (w, acc_w, prop_w, b_w) = out[capi.BN_MODE_MEGAKERNEL], out[capi.BN_MODE_WAVEFRONT]
+    assert prop_a == prop_w and b_a == b_w and b_a > 0
+    assert acc_a == acc_w, (acc_a, acc_w)
+    ok = np.isfinite(a) & np.isfinite(w)
+    assert np.array_equal(ok, np.isfinite(a)) and a[ok].sum() > 0
+    np.testing.assert_allclose(w[ok], a[ok], rtol=1e-4, atol=1e-5)
