@@ -176,7 +176,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
     for (int a = 0; a < 3; ++a) {
       const float ext = ctx->scene_hi[a] - ctx->scene_lo[a];
       lo[a] = ctx->scene_lo[a];
-      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : 64.f) / ext : 0.f;
+      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : 128.f) / ext : 0.f;
     }
     p.key_lo = make_float4(lo[0], lo[1], lo[2], 0.f);
     p.key_scale = make_float4(sc[0], sc[1], sc[2], 0.f);

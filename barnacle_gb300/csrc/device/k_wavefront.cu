@@ -59,25 +59,25 @@ __device__ __forceinline__ int find_view(const WfParams& p, long long id) {
   return v;
 }
 
-// Sort key of a ray: direction octant over the Morton code of the origin's cell in a 64 x 8 x 64
+// Sort key of a ray: direction octant over the Morton code of the origin's cell in a 128 x 8 x 128
 // grid over the scene bounds.  Rays next to each other in key order start in the same region in
 // the same octant, so a warp of them walks much the same nodes.
 __device__ __forceinline__ int ray_key(const WfParams& p, V3 o, V3 d) {
   // fmaxf maps a NaN coordinate to cell 0
-  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), 63.f));
+  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), 127.f));
   const unsigned y = static_cast<unsigned>(fminf(fmaxf((o.y - p.key_lo.y) * p.key_scale.y, 0.f), 7.f));
-  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), 63.f));
-  // interleave x5 z5 y2 x4 z4 y1 x3 z3 y0 x2 z2 x1 z1 x0 z0 (15 bits)
+  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), 127.f));
+  // interleave x6 z6 y2 x5 z5 y1 x4 z4 y0 x3 z3 x2 z2 x1 z1 x0 z0 (17 bits)
   unsigned m = 0;
   int b = 0;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
+  for (int k = 0; k < 7; ++k) {
     m |= ((z >> k) & 1u) << b++;
     m |= ((x >> k) & 1u) << b++;
-    if (k >= 3) m |= ((y >> (k - 3)) & 1u) << b++;
+    if (k >= 4) m |= ((y >> (k - 4)) & 1u) << b++;
   }
   const unsigned oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
-  return static_cast<int>((oct << 15) | m);
+  return static_cast<int>((oct << 17) | m);
 }
 
 // histogram of the keys of the lanes with pred; lanes with equal keys share one atomic.  Called
