@@ -380,10 +380,10 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
     if (w->tuned_generation[wt] != ctx->scene_generation) {
       // autotune on a truncated render of the same views: pool size (the queue width) x
       // blocks-per-SM cap, then the lanes a traversal warp refills at (the width of its batch)
-      const int pools[5] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24};
+      const int pools[6] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25};
       const int caps[2] = {0, 2};
       const int refills[3] = {16, 12, 20};
-      const long long sample = std::min<long long>(total, 32LL << 20);  // two fills of the largest pool
+      const long long sample = std::min<long long>(total, 64LL << 20);  // two fills of the largest pool
       float best = 1e30f;
       w->tuned_refill[wt] = 16;
       for (int pi : pools)
