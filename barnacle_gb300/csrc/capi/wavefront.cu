@@ -176,7 +176,7 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
     for (int a = 0; a < 3; ++a) {
       const float ext = ctx->scene_hi[a] - ctx->scene_lo[a];
       lo[a] = ctx->scene_lo[a];
-      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : 128.f) / ext : 0.f;
+      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : 256.f) / ext : 0.f;
     }
     p.key_lo = make_float4(lo[0], lo[1], lo[2], 0.f);
     p.key_scale = make_float4(sc[0], sc[1], sc[2], 0.f);
@@ -380,14 +380,16 @@ int render_wavefront(bn_context* ctx, const bn_render_desc* d, const std::vector
     if (w->tuned_generation[wt] != ctx->scene_generation) {
       // autotune on a truncated render of the same views: pool size (the queue width) x
       // blocks-per-SM cap, then the lanes a traversal warp refills at (the width of its batch)
-      const int pools[6] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25};
+      const int pools[7] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26};
       const int caps[2] = {0, 2};
       const int refills[3] = {16, 12, 20};
-      const long long sample = std::min<long long>(total, 64LL << 20);  // two fills of the largest pool
+      const long long sample = std::min<long long>(total, 128LL << 20);  // two fills of the largest pool
       float best = 1e30f;
       w->tuned_refill[wt] = 16;
       for (int pi : pools)
         for (int ci : caps) {
+          // a pool larger than the paths it would hold only adds slots to scan
+          if (pi > (1 << 20) && pi > sample) continue;
           float ms = 0.f;
           const int rc = run(ctx, w, d, pixels, sample, static_cast<int>(views.size()), pi, ci, 16, use_graph, &ms);
           if (rc) return rc;

@@ -59,25 +59,25 @@ __device__ __forceinline__ int find_view(const WfParams& p, long long id) {
   return v;
 }
 
-// Sort key of a ray: direction octant over the Morton code of the origin's cell in a 128 x 8 x 128
+// Sort key of a ray: direction octant over the Morton code of the origin's cell in a 256 x 8 x 256
 // grid over the scene bounds.  Rays next to each other in key order start in the same region in
 // the same octant, so a warp of them walks much the same nodes.
 __device__ __forceinline__ int ray_key(const WfParams& p, V3 o, V3 d) {
   // fmaxf maps a NaN coordinate to cell 0
-  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), 127.f));
+  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), 255.f));
   const unsigned y = static_cast<unsigned>(fminf(fmaxf((o.y - p.key_lo.y) * p.key_scale.y, 0.f), 7.f));
-  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), 127.f));
-  // interleave x6 z6 y2 x5 z5 y1 x4 z4 y0 x3 z3 x2 z2 x1 z1 x0 z0 (17 bits)
+  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), 255.f));
+  // interleave x7 z7 y2 x6 z6 y1 x5 z5 y0 x4 z4 ... x0 z0 (19 bits)
   unsigned m = 0;
   int b = 0;
 #pragma unroll
-  for (int k = 0; k < 7; ++k) {
+  for (int k = 0; k < 8; ++k) {
     m |= ((z >> k) & 1u) << b++;
     m |= ((x >> k) & 1u) << b++;
-    if (k >= 4) m |= ((y >> (k - 4)) & 1u) << b++;
+    if (k >= 5) m |= ((y >> (k - 5)) & 1u) << b++;
   }
   const unsigned oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
-  return static_cast<int>((oct << 17) | m);
+  return static_cast<int>((oct << 19) | m);
 }
 
 // histogram of the keys of the lanes with pred; lanes with equal keys share one atomic.  Called

@@ -8,9 +8,9 @@
 namespace bn {
 
 constexpr int kNumBins = 6;  // 4 material types, miss, no material
-// ray-queue sort keys: direction octant (3 bits) over the Morton code (17 bits) of the origin's
-// cell in a 128 x 8 x 128 grid (x, y, z) over the scene bounds
-constexpr int kSortBits = 20, kSortBins = 1 << kSortBits;
+// ray-queue sort keys: direction octant (3 bits) over the Morton code (19 bits) of the origin's
+// cell in a 256 x 8 x 256 grid (x, y, z) over the scene bounds
+constexpr int kSortBits = 22, kSortBins = 1 << kSortBits;
 enum : int {
   kCntActive = 0,   // ray-queue length
   kCntShadow = 1,   // shadow-queue length
