@@ -214,8 +214,9 @@ typedef struct bn_render_desc {
   float sigma;               /* Gaussian mutation sigma                              */
   float eps_min, eps_max;    /* Kelemen s1, s2                                       */
   /* wavefront launch shape (0 = autotuned or default) */
-  int32_t block_size;
-  int32_t queue_capacity;
+  int32_t block_size;        /* traversal blocks per SM cap                           */
+  int32_t queue_capacity;    /* path slots, 224 B of device memory each; autotuned    */
+                             /* from 1 M to 64 M slots, none beyond the render's paths */
   int32_t pad_;
 } bn_render_desc;
 
