@@ -138,9 +138,11 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
   // (ray queue only) and 107.9 (neither)
   const bool sort = true, sort_shadow = true;
   const bool count = d->flags & BN_RENDER_COUNT;
+  const int key_bits = bn::sort_key_bits(pool);
   if (w->shape_cap != cap || w->shape.watertight != wt || w->shape.wide != wide || w->shape.sort != sort ||
-      w->shape.sort_shadow != sort_shadow || w->shape.count != count || w->shape.mlt) {
-    w->shape = bn::wf_launch_shape(wt, wide, sort, sort_shadow, count, cap);
+      w->shape.sort_shadow != sort_shadow || w->shape.count != count || w->shape.mlt ||
+      w->shape.sort_tiles != (1 << (2 * key_bits + 6)) / 1024) {
+    w->shape = bn::wf_launch_shape(wt, wide, sort, sort_shadow, count, cap, false, false, 0, key_bits);
     w->shape_cap = cap;
     if (w->exec) {
       cudaGraphExecDestroy(w->exec);
@@ -176,10 +178,11 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
     for (int a = 0; a < 3; ++a) {
       const float ext = ctx->scene_hi[a] - ctx->scene_lo[a];
       lo[a] = ctx->scene_lo[a];
-      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : 256.f) / ext : 0.f;
+      sc[a] = ext > 0.f && std::isfinite(ext) ? (a == 1 ? 8.f : static_cast<float>(1 << key_bits)) / ext : 0.f;
     }
     p.key_lo = make_float4(lo[0], lo[1], lo[2], 0.f);
     p.key_scale = make_float4(sc[0], sc[1], sc[2], 0.f);
+    p.key_bits = key_bits;
   }
   p.slot_key = w->slot_key.as<int>();
   p.q_key = w->q_key.as<int>();
@@ -295,6 +298,7 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
   p.q_active = w->q_active.as<int>();
   p.sort = 0;
   p.sort_shadow = 0;
+  p.key_bits = 5;
   p.q_ray = w->q_active.as<int>();
   p.q_bins = w->q_bins.as<int>();
   p.shadow = w->shadow.as<float4>();

@@ -59,25 +59,26 @@ __device__ __forceinline__ int find_view(const WfParams& p, long long id) {
   return v;
 }
 
-// Sort key of a ray: direction octant over the Morton code of the origin's cell in a 256 x 8 x 256
-// grid over the scene bounds.  Rays next to each other in key order start in the same region in
-// the same octant, so a warp of them walks much the same nodes.
+// Sort key of a ray: direction octant over the Morton code of the origin's cell in a
+// 2^b x 8 x 2^b grid over the scene bounds (b = p.key_bits).  Rays next to each other in key order
+// start in the same region in the same octant, so a warp of them walks much the same nodes.
 __device__ __forceinline__ int ray_key(const WfParams& p, V3 o, V3 d) {
+  const int nb = p.key_bits;
+  const float top = static_cast<float>((1 << nb) - 1);
   // fmaxf maps a NaN coordinate to cell 0
-  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), 255.f));
+  const unsigned x = static_cast<unsigned>(fminf(fmaxf((o.x - p.key_lo.x) * p.key_scale.x, 0.f), top));
   const unsigned y = static_cast<unsigned>(fminf(fmaxf((o.y - p.key_lo.y) * p.key_scale.y, 0.f), 7.f));
-  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), 255.f));
-  // interleave x7 z7 y2 x6 z6 y1 x5 z5 y0 x4 z4 ... x0 z0 (19 bits)
+  const unsigned z = static_cast<unsigned>(fminf(fmaxf((o.z - p.key_lo.z) * p.key_scale.z, 0.f), top));
+  // interleave x(b-1) z(b-1) y2 x(b-2) z(b-2) y1 x(b-3) z(b-3) y0 ... x0 z0 (2b + 3 bits)
   unsigned m = 0;
   int b = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < nb; ++k) {
     m |= ((z >> k) & 1u) << b++;
     m |= ((x >> k) & 1u) << b++;
-    if (k >= 5) m |= ((y >> (k - 5)) & 1u) << b++;
+    if (k >= nb - 3) m |= ((y >> (k - (nb - 3))) & 1u) << b++;
   }
   const unsigned oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
-  return static_cast<int>((oct << 19) | m);
+  return static_cast<int>((oct << b) | m);
 }
 
 // histogram of the keys of the lanes with pred; lanes with equal keys share one atomic.  Called
@@ -547,10 +548,10 @@ __global__ void __launch_bounds__(128, kShadowBlocks) k_wf_shadow(const WfParams
   if (kWalk == kWalkCount) add_trace_counts(p.trace_counters, nrays, tc);
 }
 
-// counting sort, steps 1-2: bucket offsets = exclusive scan of the counts, over kSortBins / 1024
-// tiles of 1024 bins (one block each): step 1 sums every tile, step 2 scans its tile on top of
-// the sums of the tiles before it and clears the counts for the next use
-constexpr int kScanTiles = kSortBins / 1024;
+// counting sort, steps 1-2: bucket offsets = exclusive scan of the counts of the keys' 2^(2b + 6)
+// bins, in tiles of 1024 bins (one block each, WfLaunch::sort_tiles): step 1 sums every tile,
+// step 2 scans its tile on top of the sums of the tiles before it and clears the counts for the
+// next use
 
 __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned* total) {
   __shared__ unsigned warp_sum[32];
@@ -675,8 +676,8 @@ cudaError_t wf_launch_iteration(WfParams* dparams, const WfLaunch& l, bool use_g
                                 const WfFork* fk) {
   auto sort = [&](int shadow_queue) {
     if (!l.sort || (shadow_queue && !l.sort_shadow)) return;
-    k_wf_sort_tiles<<<kScanTiles, 1024, 0, st>>>(dparams);
-    k_wf_sort_scan<<<kScanTiles, 1024, 0, st>>>(dparams);
+    k_wf_sort_tiles<<<l.sort_tiles, 1024, 0, st>>>(dparams);
+    k_wf_sort_scan<<<l.sort_tiles, 1024, 0, st>>>(dparams);
     k_wf_sort_scatter<<<l.grid_scatter, 256, 0, st>>>(dparams, shadow_queue);
   };
   cudaError_t e = cudaSuccess;
@@ -733,8 +734,9 @@ cudaError_t wf_launch_resolve(WfParams* dparams, cudaStream_t st) {
 }
 
 WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
-                         bool mlt, bool mlt_kelemen, long long mlt_chains) {
+                         bool mlt, bool mlt_kelemen, long long mlt_chains, int key_bits) {
   WfLaunch l{};
+  l.sort_tiles = (1 << (2 * key_bits + 6)) / 1024;
   l.mlt = mlt;
   l.mlt_kelemen = mlt_kelemen;
   l.watertight = watertight;

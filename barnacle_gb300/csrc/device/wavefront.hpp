@@ -8,9 +8,20 @@
 namespace bn {
 
 constexpr int kNumBins = 6;  // 4 material types, miss, no material
-// ray-queue sort keys: direction octant (3 bits) over the Morton code (19 bits) of the origin's
-// cell in a 256 x 8 x 256 grid (x, y, z) over the scene bounds
+// ray-queue sort keys: direction octant (3 bits) over the Morton code of the origin's cell in a
+// 2^b x 8 x 2^b grid (x, y, z) over the scene bounds, b from 5 to 8 with the pool (sort_key_bits):
+// at most 22 bits
 constexpr int kSortBits = 22, kSortBins = 1 << kSortBits;
+// b for a pool of path slots: the histogram's fixed scan cost (two passes over its bins per sort)
+// grows with the bins, the sort's coherence with the rays per bin.  Measured on the 1,024-instance
+// workload: 16-bit keys (b = 5) best at 1 M slots, 20-bit (b = 7) at 16 M, 22-bit (b = 8) at 32 M
+// and 64 M
+inline int sort_key_bits(long long pool) {
+  int lg = 0;
+  while ((2LL << lg) <= pool) ++lg;  // floor(log2(pool))
+  const int b = (lg - 9) / 2;
+  return b < 5 ? 5 : (b > 8 ? 8 : b);
+}
 enum : int {
   kCntActive = 0,   // ray-queue length
   kCntShadow = 1,   // shadow-queue length
@@ -69,7 +80,8 @@ struct WfParams {
   int* q_bins;                  // kNumBins x pool entries
   // spatial sort of both ray queues (counting sort by key, when sort != 0)
   int sort, sort_shadow;
-  float4 key_lo, key_scale;     // origin cell = (o - key_lo) * key_scale, in [0, 32) x [0, 8) x [0, 32)
+  float4 key_lo, key_scale;     // origin cell = (o - key_lo) * key_scale, in [0, 2^b) x [0, 8) x [0, 2^b)
+  int key_bits;                 // b (sort_key_bits): the keys span 2^(2b + 6) bins
   int* slot_key;                // per slot: key of the ray the slot holds (written by shade)
   int* q_key;                   // per ray-queue entry: its key
   int* q_ray;                   // the ray queue in key order (read by extend)
@@ -90,6 +102,7 @@ struct WfParams {
 
 struct WfLaunch {
   int grid_regen, grid_extend, grid_shade, grid_shadow, grid_scatter;
+  int sort_tiles;               // 1,024-bin tiles of the keys' histogram (2^(2b + 6) / 1,024)
   bool watertight;
   bool wide;                    // the scene's wide records (kWalkWide kernels)
   bool sort, sort_shadow;       // ray / shadow queue sorted by ray key before extend / shadow
@@ -100,7 +113,7 @@ struct WfLaunch {
 
 // mlt_chains: PSSMLT chains (one slot each); sizes the traversal grids so both fit side by side
 WfLaunch wf_launch_shape(bool watertight, bool wide, bool sort, bool sort_shadow, bool count, int blocks_per_sm_cap,
-                         bool mlt = false, bool mlt_kelemen = false, long long mlt_chains = 0);
+                         bool mlt = false, bool mlt_kelemen = false, long long mlt_chains = 0, int key_bits = 5);
 // the chain kernels of the PSSMLT wavefront (k_mlt_wavefront.cu)
 cudaError_t mlt_launch_regen(WfParams* dparams, int grid, bool kelemen, cudaStream_t st);
 cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, bool kelemen, cudaStream_t st);
