@@ -66,6 +66,24 @@ def test_wavefront_small_pool_regenerates_correctly(ctx, pool):
     assert_same_image(wave, mega)
 
 
+@pytest.mark.parametrize("pool", [1 << 20, 1 << 21, 1 << 23, 1 << 25])
+def test_wavefront_sort_key_widths(ctx, pool):
+    """The queues' sort keys have 16, 18, 20 and 22 bits at these pools (2^b x 8 x 2^b origin
+    cells under the octant, b following the pool): sorting only reorders the rays, so every width
+    gives the megakernel's image up to summation order, on the instanced scene whose keys spread
+    over the most cells."""
+    b = Bundle.generate("instances", 1)
+    ctx.upload(b)
+    views = b.views[:2]
+    for v in views:
+        v.width, v.height = v.width // 4, v.height // 4
+    mega = render(ctx, b, views, 2, capi.BN_MODE_MEGAKERNEL)
+    wave = render(ctx, b, views, 2, capi.BN_MODE_WAVEFRONT, pool=pool)
+    for m, w in zip(mega, wave):
+        assert float(m.sum()) > 0
+        assert_same_image(w, m)
+
+
 def test_wavefront_many_views_one_launch(ctx):
     b = Bundle.generate("instances", 1)
     ctx.upload(b)
