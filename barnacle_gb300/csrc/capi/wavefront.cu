@@ -88,8 +88,8 @@ cudaError_t ensure_pool(WfState* w, int pool) {
   return cudaSuccess;
 }
 
-// the while-node graph: body = one iteration (regen, extend, shade, shadow, control; for PSSMLT
-// chains shadow and extend as two branches, then shade, regen, control)
+// the while-node graph of the path tracer: body = one iteration (regen, extend, shade, shadow,
+// control)
 int build_graph(bn_context* ctx, WfState* w) {
   if (w->exec) {
     cudaGraphExecDestroy(w->exec);
@@ -115,8 +115,7 @@ int build_graph(bn_context* ctx, WfState* w) {
   if ((e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
       cudaSuccess)
     return ctx->cuda_fail(e, "cudaStreamBeginCaptureToGraph");
-  cudaError_t le = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, true, ctx->stream,
-                                           w->shape.mlt ? &w->fork : nullptr);
+  cudaError_t le = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, true, ctx->stream);
   cudaGraph_t captured = body;
   e = cudaStreamEndCapture(ctx->stream, &captured);
   if (le != cudaSuccess) return ctx->cuda_fail(le, "capture of the bounce loop");
@@ -247,8 +246,10 @@ int run(bn_context* ctx, WfState* w, const bn_render_desc* d, long long n_pixels
 }
 
 // The bounce loop of PSSMLT chains (one slot per chain), enqueued on the context's stream after
-// the bootstrap: a graph launch, or host-driven iterations with BN_RENDER_NO_GRAPH.  Splats go
-// straight into ctx->film.  Returns the iterations run through *iters.
+// the bootstrap as host-driven iterations: a render of 65,536 chains runs about 2,100 short ones,
+// and measured at 1024^2 they took 435-454 ms as launches from the host against 489-500 ms as the
+// iterations of a conditional graph node.  Splats go straight into ctx->film.  Returns the
+// iterations run through *iters.
 int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltParams& mp, int* iters) {
   cudaError_t e;
   const int pool = mp.n_chains;
@@ -271,7 +272,6 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
       w->exec = nullptr;
     }
   }
-  bool use_graph = !(d->flags & BN_RENDER_NO_GRAPH);
   bn::WfParams p{};
   p.scene = ctx->scene;
   p.views = mp.view;
@@ -326,29 +326,19 @@ int run_mlt(bn_context* ctx, WfState* w, const bn_render_desc* d, const bn::MltP
   q.X = mp.X;
   q.film = mp.film;
   q.accepted = mp.accepted;
-  if (use_graph && !w->exec && !w->graph_failed) {
-    if (build_graph(ctx, w) != BN_OK) {
-      w->graph_failed = true;
-      use_graph = false;
-    }
-  }
-  if (use_graph && !w->exec) use_graph = false;
-  p.cond = w->cond;
   cudaStream_t st = ctx->stream;
   cudaMemcpyAsync(w->params.ptr, &p, sizeof(p), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(w->counters.ptr, 0, bn::kCntSize * sizeof(int), st);
   cudaMemsetAsync(w->meta.ptr, 0, static_cast<size_t>(pool) * sizeof(int4), st);  // every chain unstarted
-  if (use_graph) {
-    if ((e = cudaGraphLaunch(w->exec, st)) != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphLaunch");
-  } else {
-    for (int it = 0; it < p.max_iters + 1; ++it) {
-      if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st, &w->fork)) != cudaSuccess)
-        return ctx->cuda_fail(e, "wavefront chain iteration launch");
-      int again = 0;
-      cudaMemcpyAsync(&again, w->counters.as<int>() + bn::kCntAgain, sizeof(int), cudaMemcpyDeviceToHost, st);
-      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront chain iteration");
-      if (!again) break;
-    }
+  // (checking the loop condition every 4 or 16 iterations instead of every one measured slower:
+  // 499 and 510 against 450 ms)
+  for (int it = 0; it < p.max_iters + 1; ++it) {
+    if ((e = bn::wf_launch_iteration(w->params.as<bn::WfParams>(), w->shape, false, st, &w->fork)) != cudaSuccess)
+      return ctx->cuda_fail(e, "wavefront chain iteration launch");
+    int again = 0;
+    cudaMemcpyAsync(&again, w->counters.as<int>() + bn::kCntAgain, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ctx->cuda_fail(e, "wavefront chain iteration");
+    if (!again) break;
   }
   int counters[bn::kCntSize];
   e = cudaMemcpyAsync(counters, w->counters.ptr, sizeof(counters), cudaMemcpyDeviceToHost, st);

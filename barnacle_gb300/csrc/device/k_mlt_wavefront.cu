@@ -54,6 +54,7 @@ __device__ __forceinline__ MltSampler chain_sampler(const MltWf& q, int chain) {
   m.sigma = q.sigma;
   m.eps_min = q.eps_min;
   m.eps_max = q.eps_max;
+  m.log_eps = logf(__fdiv_rn(m.eps_max, m.eps_min));
   m.X = q.X + static_cast<long long>(chain) * q.n_dims;
   m.stride = 1;
   m.max_dims = q.n_dims;

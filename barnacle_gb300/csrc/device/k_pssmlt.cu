@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(128) k_mlt_chains(MltParams p) {
     m.sigma = p.sigma;
     m.eps_min = p.eps_min;
     m.eps_max = p.eps_max;
+    m.log_eps = logf(__fdiv_rn(m.eps_max, m.eps_min));
     m.X = p.X + chain;
     m.stride = p.n_chains;
     m.max_dims = p.n_dims;

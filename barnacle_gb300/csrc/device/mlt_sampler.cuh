@@ -48,6 +48,7 @@ struct MltSampler {
   float p_large;
   int kelemen;
   float sigma, eps_min, eps_max;
+  float log_eps;  // logf(eps_max / eps_min), set with them: Kelemen's exponent scale, once per chain
   float4* X;
   long long stride;
   int max_dims;
@@ -72,7 +73,7 @@ struct MltSampler {
       v = lcg_next(inner);
     } else if (kelemen) {
       v = x.x;
-      const float a = logf(__fdiv_rn(eps_max, eps_min));
+      const float a = log_eps;
       for (int k = last_mod; k < cur_iter; ++k) {
         const float u1 = __fsub_rn(lcg_next(inner), 0.5f);
         const float u2 = u1 < 0.f ? __fadd_rn(1.f, __fmul_rn(2.f, u1)) : __fmul_rn(2.f, u1);

@@ -120,7 +120,7 @@ cudaError_t mlt_launch_shade(WfParams* dparams, int grid, bool watertight, bool 
 int mlt_grid_regen();
 int mlt_grid_shade(bool watertight);
 // a second stream and two events: the PSSMLT iteration traces its shadow and extension rays on
-// two streams at once (fork / join, also inside a graph capture)
+// two streams at once (fork / join)
 struct WfFork {
   cudaStream_t side;
   cudaEvent_t fork, join;

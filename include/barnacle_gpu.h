@@ -186,6 +186,7 @@ enum bn_mutation_type { BN_MUTATION_GAUSSIAN = 0, BN_MUTATION_KELEMEN = 1 };
 #define BN_RENDER_FIXED_ALIAS 0x2u  /* PSSMLT: start chains proportional to bootstrap weight  */
                                     /* (the reference's AliasTable samples uniformly)          */
 #define BN_RENDER_NO_GRAPH 0x4u     /* wavefront: launch the bounce loop without a CUDA graph  */
+                                    /* (PSSMLT chains always run host-driven iterations)       */
 #define BN_RENDER_COUNT 0x8u        /* count rays / BVH nodes / triangles / instances visited  */
                                     /* into bn_stats (a slower instrumented kernel variant)     */
 #define BN_RENDER_CULL_SHADOW 0x10u /* megakernel: evaluate a light sample first and trace its   */

@@ -104,9 +104,9 @@ def test_pssmlt_errors(ctx):
         ctx.render(r, b.views + b.views)  # one view per PSSMLT render
 
 
-@pytest.mark.parametrize("name,kelemen,fixed,graph", [("cornell", True, False, True), ("cornell", False, True, False),
-                                                      ("cornell-objects", True, True, True)])
-def test_pssmlt_wavefront_chains_equal_lockstep(ctx, name, kelemen, fixed, graph):
+@pytest.mark.parametrize("name,kelemen,fixed", [("cornell", True, False), ("cornell", False, True),
+                                                ("cornell-objects", True, True)])
+def test_pssmlt_wavefront_chains_equal_lockstep(ctx, name, kelemen, fixed):
     """The chains compacted every bounce (BN_MODE_WAVEFRONT) draw every chain's random numbers in
     the lockstep kernel's order, so each chain makes the same mutations and the same decisions:
     the accepted count and b are identical, the films equal up to the splats' summation order."""
@@ -117,7 +117,7 @@ def test_pssmlt_wavefront_chains_equal_lockstep(ctx, name, kelemen, fixed, graph
     out = {}
     for mode in (capi.BN_MODE_MEGAKERNEL, capi.BN_MODE_WAVEFRONT):
         r.mode = mode
-        r.flags = (capi.BN_RENDER_FIXED_ALIAS if fixed else 0) | (0 if graph else capi.BN_RENDER_NO_GRAPH)
+        r.flags = capi.BN_RENDER_FIXED_ALIAS if fixed else 0
         ctx.reset_stats()
         img = ctx.render(r, v)[0]
         st = ctx.stats()
@@ -131,8 +131,8 @@ def test_pssmlt_wavefront_chains_equal_lockstep(ctx, name, kelemen, fixed, graph
     np.testing.assert_allclose(w[ok], a[ok], rtol=1e-4, atol=1e-5)
 
 
-@pytest.mark.parametrize("depth,graph", [(1, True), (1, False), (2, True)])
-def test_pssmlt_wavefront_short_paths_equal_lockstep(ctx, depth, graph):
+@pytest.mark.parametrize("depth", [1, 2])
+def test_pssmlt_wavefront_short_paths_equal_lockstep(ctx, depth):
     """Paths of one or two bounces: at depth 1 every path ends at its first bounce, most with a
     shadow record still to trace, so nearly every chain waits an iteration before its Metropolis
     step; the decisions must still be the lockstep kernel's."""
@@ -143,7 +143,7 @@ def test_pssmlt_wavefront_short_paths_equal_lockstep(ctx, depth, graph):
     out = {}
     for mode in (capi.BN_MODE_MEGAKERNEL, capi.BN_MODE_WAVEFRONT):
         r.mode = mode
-        r.flags = 0 if graph else capi.BN_RENDER_NO_GRAPH
+        r.flags = 0
         ctx.reset_stats()
         img = ctx.render(r, v)[0]
         st = ctx.stats()
