@@ -450,6 +450,28 @@ def test_bench_reads_the_committed_profile_figures():
     assert bench.profile_figures("cornell") is None
 
 
+def test_bench_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the CPU restatement, no GPU library loaded) prints one JSON line
+    with the GPU arm's metric, unit and workload config, `impl: reference`, a `cpu_baseline`
+    describing the run and an `e2e` object without host-device copies."""
+    import subprocess
+    import sys
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0", "--views", "2"], capture_output=True, text=True, timeout=600,
+                         cwd=str(ROOT))
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "paths/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["n_gpus"] == 1
+    assert d["config"]["workload"].startswith("instances") and d["config"]["views"] == 2
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and "tiles" in cb["sample"]
+    e = d["e2e"]
+    assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
 def test_bench_cpu_tiles_cover_every_view():
     """The CPU arms sample 16x16 tiles of every view, a different cell of a 4x4 grid per step;
     16 steps visit every cell of every view once."""
