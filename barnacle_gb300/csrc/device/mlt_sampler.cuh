@@ -119,8 +119,24 @@ struct MltSampler {
       u[k] = draw(i, x[k]);
     }
   }
+  // Reject restores every initialised dimension.  The records are read eight at a time before any
+  // is written back: the stride is a runtime value, so record by record each load would wait for
+  // the store before it, one memory round trip per dimension.
   __device__ __forceinline__ void reject() {
-    for (int i = 0; i < min(initialized, max_dims); ++i) {
+    const int n = min(initialized, max_dims);
+    int i = 0;
+    for (; i + 8 <= n; i += 8) {
+      float4 x[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) x[k] = X[static_cast<long long>(i + k) * stride];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        x[k].x = x[k].y;
+        x[k].z = x[k].w;
+        X[static_cast<long long>(i + k) * stride] = x[k];
+      }
+    }
+    for (; i < n; ++i) {
       float4* xp = X + static_cast<long long>(i) * stride;
       float4 x = *xp;
       x.x = x.y;
